@@ -1,0 +1,335 @@
+"""Benchmark: pull + push throughput at 192^3, cubic B-spline, DCT-II bounds, ext = 1.
+
+One step = one pull of a 192^3 Float32 image through a 192^3 deformation
+(identity + FWHM-12 smoothed random field scaled to +-5 voxels) followed by one
+push of the pulled values back through the same deformation.  ``value`` is
+Gvox/s (sample voxels x channels per second, whole job) from CUDA events around
+each step with inputs resident in HBM and L2 flushed before each step; ``e2e``
+is the same step through the reference-facing host-pointer ABI (the ``pull`` /
+``push`` symbols of artifacts/C/pushpull.h) with pinned host buffers.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+``--impl reference`` times the reference CPU implementation of the path on the
+host cores instead (compiled from the reference sources where possible, else the
+CPU port of it), on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "pull+push Gvox/s & HBM GB/s @192³ cubic; fused fwd+adjoint vs plain GPU"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic(name):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as fh:
+            return json.load(fh).get(name)
+    except Exception:
+        return None
+
+
+class Clocks:
+    """Samples nvidia-smi every 200 ms while the timed region runs."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid):
+        self.uuid, self.proc, self.path = uuid, None, None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            cmd = ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"]
+            if self.uuid:
+                cmd += ["-i", self.uuid]
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(cmd, stdout=self.fh, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path:
+            return None
+        rows = []
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 8:
+                    continue
+                try:
+                    rows.append((float(parts[0]), float(parts[1]), float(parts[2]), parts[3:]))
+                except ValueError:
+                    continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[3][1:]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": sorted(reasons)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _workload(args):
+    from pushpull_gb300 import workloads
+    w = workloads.config2(seed=args.seed)
+    return w
+
+
+def cpu_baseline(w, seconds=8.0, kind=None):
+    from oracle.cpu_bench import PullPushCPU
+    h = PullPushCPU(w.f0, w.phi, w.deg, w.bnd, w.ext, kind=kind)
+    h.step()                                   # warm-up
+    times = []
+    t_end = time.perf_counter() + seconds
+    while time.perf_counter() < t_end or len(times) < 2:
+        times.append(h.step())
+    n1 = h.n1
+    h.close()
+    sec = statistics.mean(times)
+    return {"value": n1 / sec / 1e9, "unit": "Gvox/s", "cores": h.threads, "kind": h.kind,
+            "sample": f"full workload: pull + push of all {n1} voxels per rep, {len(times)} reps "
+                      f"({sum(times):.1f} s), {h.threads} threads over contiguous voxel slabs"}, sec
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    w = _workload(args)
+    from oracle.cpu_bench import PullPushCPU
+    h = PullPushCPU(w.f0, w.phi, w.deg, w.bnd, w.ext)
+    for _ in range(args.warmup):
+        h.step()
+    times = [h.step() for _ in range(args.steps)]
+    h.close()
+    sec = statistics.mean(times)
+    value = h.n1 / sec / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Gvox/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": _config(w, args),
+            "cpu_baseline": {"value": value, "unit": "Gvox/s", "cores": h.threads, "kind": h.kind,
+                             "sample": f"pull + push of all {h.n1} voxels per step, {h.threads} threads"},
+            "e2e": {"value": value, "unit": "Gvox/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _config(w, args):
+    return {"workload": "pull then push, 192x192x192 Float32, 1 channel, degree 3 (cubic) all dims, "
+                        "DCT-II bounds, extrapolate=true, phi = identity + FWHM-12 smoothed N(0,1) field "
+                        "scaled to +-5 vox",
+            "d": list(w.f0.shape[:3]), "deg": list(w.deg), "bnd": w.bnd, "ext": w.ext, "channels": 1,
+            "seed": args.seed,
+            "l2": f"flushed before every step by a {L2_FLUSH_BYTES >> 20} MiB write outside the step's events"}
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    import __graft_entry__ as entry
+    pkg = entry.package()
+    L = pkg.layout
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    w = _workload(args)
+    d0 = tuple(w.f0.shape[:3])
+    d1 = tuple(w.phi.shape[:3])
+    n0, n1 = int(np.prod(d0)), int(np.prod(d1))
+    nc = 1
+    s = pkg.Settings(w.deg, w.bnd, w.ext)
+    f0 = L.from_numpy(w.f0, dev)
+    phi = L.from_numpy(w.phi, dev)
+    f1 = L.empty(d1, device=dev)
+    acc = L.empty(d0, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def step(evs=None):
+        flush.fill_(1.0)
+        if evs:
+            evs[0].record()
+        pkg.pull(f0, phi, s, out=f1)
+        if evs:
+            evs[1].record()
+        pkg.push(f1, phi, d0, s, out=acc, accumulate=False)
+        if evs:
+            evs[2].record()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    uuid = None
+    try:
+        uuid = str(torch.cuda.get_device_properties(dev).uuid)
+        uuid = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+    except Exception:
+        pass
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(uuid if rank == 0 else None) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            step(evs[i])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if ws > 1:
+        dist.barrier()
+    pull_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    push_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    step_ms = statistics.mean(a + b for a, b in zip(pull_ms, push_ms))
+    if ws > 1:
+        t = torch.tensor([step_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = ws * n1 * nc / (step_ms * 1e-3) / 1e9
+
+    # ---- end to end through the reference-facing host ABI (pinned host buffers)
+    e2e = None
+    if not args.no_e2e:
+        import ctypes as C
+        lib = pkg.native_library()
+        hf0 = torch.from_numpy(np.ascontiguousarray(w.f0.ravel(order="F"))).pin_memory()
+        hphi = torch.from_numpy(np.ascontiguousarray(w.phi.ravel(order="F"))).pin_memory()
+        hf1 = torch.empty(n1, dtype=torch.float32).pin_memory()
+        hacc = torch.empty(n0, dtype=torch.float32).pin_memory()
+        cd0 = (C.c_ulonglong * 3)(*d0)
+        cb = (C.c_int * 3)(*((w.bnd,) * 3 if isinstance(w.bnd, int) else w.bnd))
+        cdp = (C.c_ulonglong * 3)(*[d + 1 for d in w.deg])
+
+        def host_step():
+            lib.pull(hf1.data_ptr(), hphi.data_ptr(), hf0.data_ptr(), C.cast(cd0, C.c_void_p), n1,
+                     C.cast(cb, C.c_void_p), C.cast(cdp, C.c_void_p), w.ext)
+            hacc.zero_()                              # caller zero-fills, src/pushpull_cpu.jl:190
+            lib.push(hacc.data_ptr(), hphi.data_ptr(), hf1.data_ptr(), C.cast(cd0, C.c_void_p), n1,
+                     C.cast(cb, C.c_void_p), C.cast(cdp, C.c_void_p), w.ext)
+
+        for _ in range(max(args.warmup, 3)):
+            host_step()
+        if ws > 1:
+            dist.barrier()
+        te = time.perf_counter()
+        for _ in range(args.steps):
+            host_step()
+        e2e_s = (time.perf_counter() - te) / args.steps
+        if ws > 1:
+            t = torch.tensor([e2e_s], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": ws * n1 * nc / e2e_s / 1e9, "unit": "Gvox/s",
+               "h2d_bytes_per_step": (12 * n1 + 4 * n0) + (12 * n1 + 4 * n1 + 4 * n0),
+               "d2h_bytes_per_step": 4 * n1 + 4 * n0,
+               "ms_per_step": e2e_s * 1e3,
+               "path": "host-pointer ABI pull() then push() (artifacts/C/pushpull.h signatures)"}
+
+    if rank != 0:
+        if ws > 1:
+            dist.destroy_process_group()
+        return 0
+
+    peak, peak_src = _peaks()
+    bytes_pull = 12 * n1 + 4 * nc * n0 + 4 * nc * n1
+    bytes_push = 12 * n1 + 4 * nc * n1 + 4 * nc * n0
+    mp, mq = statistics.mean(pull_ms), statistics.mean(push_ms)
+    dom, dom_ms, dom_bytes = ("push", mq, bytes_push) if mq >= mp else ("pull", mp, bytes_pull)
+    ach = dom_bytes / (dom_ms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+            "frac": ach / peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+            "algorithmic_bytes_per_launch": dom_bytes, "traffic": _traffic(dom)}
+    kernels = {
+        "pull": {"ms": mp, "GB_s": bytes_pull / (mp * 1e-3) / 1e9, "frac_of_peak": bytes_pull / (mp * 1e-3) / 1e9 / peak,
+                 "Gvox_s": n1 / (mp * 1e-3) / 1e9},
+        "push": {"ms": mq, "GB_s": bytes_push / (mq * 1e-3) / 1e9, "frac_of_peak": bytes_push / (mq * 1e-3) / 1e9 / peak,
+                 "Gvox_s": n1 / (mq * 1e-3) / 1e9},
+        "pull+push_frac_of_peak": (bytes_pull + bytes_push) / ((mp + mq) * 1e-3) / 1e9 / peak,
+    }
+    cpu = None
+    if not args.no_cpu and ws == 1 or (not args.no_cpu and rank == 0):
+        cpu, _ = cpu_baseline(w, seconds=args.cpu_seconds)
+    line = {"metric": METRIC, "value": value, "unit": "Gvox/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded): smoothed U(0,1) image, smoothed "
+            "random displacement", "config": _config(w, args), "roofline": roof, "cpu_baseline": cpu,
+            "e2e": e2e, "gpu_launches": 2 * args.steps, "clocks": clk.summary(), "kernels": kernels,
+            "wall_s_timed_region": wall}
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    args = ap.parse_args(argv)
+    import __graft_entry__ as entry
+    entry.package()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

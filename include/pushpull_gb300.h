@@ -1,0 +1,126 @@
+/*
+ * pushpull_gb300.h -- C ABI of the GB300 B-spline pull / push library.
+ *
+ * Two layers, both plain C types (no CUDA or torch types in any signature):
+ *
+ * 1. Native layer (pp_*): DEVICE pointers, the whole (channel, batch) set in
+ *    one stream-ordered call, status codes.  This is what the CUDA-side
+ *    binding calls: it replaces the CUDA.jl extension's per-(channel, batch)
+ *    cudacall of the reference PTX kernels (ext/pushpull_gpu.jl:15-259) and its
+ *    module-global __constant__ settings (ext/pushpull_gpu.jl:268-274, 380-383).
+ *
+ * 2. Compatibility layer: the exact symbols and signatures of the reference's
+ *    CPU library (artifacts/C/pushpull.h:1-14, plus pullh at pushpull.c:111)
+ *    on HOST pointers, one (channel, batch) slice per call, so the reference's
+ *    own ccall sites (src/pushpull_cpu.jl:45, 100, 140, 195, 251, 294, 337)
+ *    bind to this library unchanged.  Each call copies its inputs to the
+ *    device, runs the GB300 kernel and copies the result back before returning.
+ *
+ * Array layout everywhere is the reference's Julia column-major layout:
+ *   image      f   (d0[0], d0[1], d0[2], nc, nb)
+ *   deformation phi (d1[0], d1[1], d1[2], 3, nb), 1-based voxel coordinates,
+ *                   component k of voxel i at phi[i + k*n1]
+ *   samples    f1  (d1[0], d1[1], d1[2], nc, nb)
+ *   gradients  g   (d1[0], d1[1], d1[2], 3, nc, nb)
+ *   Hessians   h   (d1[0], d1[1], d1[2], 3, 3, nc, nb)
+ * Settings: deg[k] in 0..4 per dimension; boundary codes 0 circulant,
+ * 1 reflect (DCT-II), 2 antisymmetric reflect (DST-II), three per channel
+ * (nbnd == 1: one triple for every channel, nbnd == nc: one per channel);
+ * ext 0/1 (src/pushpull_general.jl:15-60).
+ *
+ * Thread safety: native calls keep no state besides the thread-local error
+ * string and are safe from any thread on any stream.  Compatibility calls use
+ * a per-thread device workspace and stream.
+ */
+#ifndef PUSHPULL_GB300_H
+#define PUSHPULL_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef unsigned long long pp_usize;   /* USIZE_t of artifacts/C/pushpull.h:1 */
+
+enum pp_status {
+    PP_OK = 0,
+    PP_ERR_NULL = 1,          /* a required pointer is NULL                         */
+    PP_ERR_DIMS = 2,          /* a dimension is zero where data is needed / overflow */
+    PP_ERR_DEGREE = 3,        /* degree outside 0..4                                 */
+    PP_ERR_BOUND = 4,         /* boundary code outside {0,1,2}                       */
+    PP_ERR_CHANNELS = 5,      /* nc/nb < 1 or nbnd not in {1, nc}                    */
+    PP_ERR_ALIGN = 6,         /* float pointer not 4-byte aligned                    */
+    PP_ERR_CUDA = 7,          /* a CUDA runtime call failed                          */
+    PP_ERR_UNSUPPORTED = 8,   /* request outside what this build supports            */
+    PP_ERR_TOO_LARGE = 9,     /* request exceeds a fixed capacity                    */
+    PP_ERR_TIMEOUT = 10       /* a bounded device-side wait gave up                  */
+};
+
+/* ------------------------------------------------------------------------ */
+/* Native layer: device pointers, stream ordered (stream = cudaStream_t or 0) */
+/* ------------------------------------------------------------------------ */
+
+/* f1 = pull(f0, phi): replaces pull (src/pushpull_cpu.jl:17-53,
+ * ext/pushpull_gpu.jl:15-51; per-voxel pull, artifacts/C/pushpull.c:55-74).
+ * Invalid voxels (non-finite phi, or outside the band when ext == 0) get NaN. */
+int pp_pull(float *f1, const float *phi, const float *f0,
+            const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
+            const int *bnd, int nbnd, const int deg[3], int ext, void *stream);
+
+/* g1 = pull_grad(f0, phi), 3 planar components per channel: replaces pull_grad
+ * (src/pushpull_cpu.jl:69-108, ext/pushpull_gpu.jl:66-101; pullg, pushpull.c:78-107). */
+int pp_pull_grad(float *g1, const float *phi, const float *f0,
+                 const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
+                 const int *bnd, int nbnd, const int deg[3], int ext, void *stream);
+
+/* h1 = pull_hess(f0, phi), symmetric 3x3 (9 planar components) per channel:
+ * replaces pull_hess (src/pushpull_cpu.jl:111-148; pullh, pushpull.c:111-143). */
+int pp_pull_hess(float *h1, const float *phi, const float *f0,
+                 const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
+                 const int *bnd, int nbnd, const int deg[3], int ext, void *stream);
+
+/* f0 (+)= push(f1, phi): replaces push (src/pushpull_cpu.jl:165-203,
+ * ext/pushpull_gpu.jl:165-201; push, pushpull.c:147-164).  accumulate != 0 adds
+ * into the caller's f0 (the reference contract: the caller zero-fills);
+ * accumulate == 0 zeroes f0 on the stream first.  Non-finite f1 values and
+ * invalid voxels are skipped. */
+int pp_push(float *f0, const float *phi, const float *f1,
+            const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
+            const int *bnd, int nbnd, const int deg[3], int ext,
+            int accumulate, void *stream);
+
+/* g0 (+)= push_grad(g1, phi), the adjoint of pull_grad: replaces push_grad
+ * (src/pushpull_cpu.jl:220-259, ext/pushpull_gpu.jl:220-259; pushg_element,
+ * artifacts/C/pushpull.cu:145-163).  Voxels with a non-finite gradient
+ * component are skipped. */
+int pp_push_grad(float *g0, const float *phi, const float *g1,
+                 const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
+                 const int *bnd, int nbnd, const int deg[3], int ext,
+                 int accumulate, void *stream);
+
+/* Message of the last failing call on this thread ("" when none). */
+const char *pp_last_error(void);
+
+/* Library version: major*10000 + minor*100 + patch. */
+int pp_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Compatibility layer: the reference CPU ABI on HOST pointers                */
+/* (artifacts/C/pushpull.h:3-14).  dp[k] = degree + 1; n1 = sample voxels.    */
+/* On failure nothing is written, a message goes to stderr and to             */
+/* pp_last_error().                                                           */
+/* ------------------------------------------------------------------------ */
+void pull (float *f1, const float *phi, const float *f0,
+           const pp_usize *d0, const pp_usize n1, const int *bnd, const pp_usize *dp, const int ext);
+void pullg(float *g1, const float *phi, const float *f0,
+           const pp_usize *d0, const pp_usize n1, const int *bnd, const pp_usize *dp, const int ext);
+void pullh(float *h1, const float *phi, const float *f0,
+           const pp_usize *d0, const pp_usize n1, const int *bnd, const pp_usize *dp, const int ext);
+void push (float *f0, const float *phi, const float *f1,
+           const pp_usize *d0, const pp_usize n1, const int *bnd, const pp_usize *dp, const int ext);
+void pushg(float *g0, const float *phi, const float *g1,
+           const pp_usize *d0, const pp_usize n1, const int *bnd, const pp_usize *dp, const int ext);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PUSHPULL_GB300_H */

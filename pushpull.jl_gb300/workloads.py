@@ -1,0 +1,118 @@
+"""Seeded synthetic volumes and deformations for the benchmark workloads.
+
+No public dataset is involved; these stand in for the workloads with the stated
+shapes and value distributions:
+
+* images: i.i.d. U(0,1), Gaussian-smoothed (FWHM in voxels, sigma = FWHM/2.3548,
+  periodic boundary);
+* deformations: 1-based identity plus a displacement made of one seeded N(0,1)
+  field per component, smoothed, then scaled so that max|u| equals the stated
+  amplitude (optionally composed with a global contraction about the centre).
+
+Everything is Float32 in the reference's column-major layout (numpy Fortran order).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+FWHM_TO_SIGMA = 1.0 / 2.3548
+
+
+def _smooth(a: np.ndarray, fwhm: float) -> np.ndarray:
+    from scipy.ndimage import gaussian_filter
+    return gaussian_filter(a, sigma=fwhm * FWHM_TO_SIGMA, mode="wrap")
+
+
+def image(d, seed: int, fwhm: float = 3.0, channels: int = 1) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    vols = [_smooth(rng.random(tuple(d)).astype(np.float32), fwhm) for _ in range(channels)]
+    out = np.stack(vols, axis=-1) if channels > 1 else vols[0]
+    return np.asfortranarray(out.astype(np.float32))
+
+
+def identity(d) -> np.ndarray:
+    x = np.arange(1, d[0] + 1, dtype=np.float32)[:, None, None]
+    y = np.arange(1, d[1] + 1, dtype=np.float32)[None, :, None]
+    z = np.arange(1, d[2] + 1, dtype=np.float32)[None, None, :]
+    phi = np.empty(tuple(d) + (3,), dtype=np.float32, order="F")
+    phi[..., 0], phi[..., 1], phi[..., 2] = x, y, z
+    return phi
+
+
+def deformation(d, seed: int, fwhm: float, amplitude: float, contraction: float = 1.0,
+                d_src=None) -> np.ndarray:
+    """identity (optionally scaled by ``contraction`` about the centre of ``d_src``)
+    plus a smoothed random field with max|u| = amplitude."""
+    rng = np.random.default_rng(seed)
+    d = tuple(int(v) for v in d)
+    d_src = tuple(int(v) for v in (d_src or d))
+    phi = identity(d).astype(np.float64)
+    for k in range(3):
+        # map the sample grid onto the source grid, then contract about its centre
+        scale = (d_src[k] - 1) / max(d[k] - 1, 1)
+        x = 1.0 + (phi[..., k] - 1.0) * scale
+        c = 0.5 * (d_src[k] + 1)
+        phi[..., k] = c + contraction * (x - c)
+    u = np.stack([_smooth(rng.standard_normal(d).astype(np.float32), fwhm) for _ in range(3)], axis=-1)
+    m = float(np.abs(u).max())
+    if m > 0:
+        u *= amplitude / m
+    return np.asfortranarray((phi + u).astype(np.float32))
+
+
+@dataclass
+class Workload:
+    name: str
+    f0: np.ndarray          # (d0..., [C])
+    phi: np.ndarray         # (d1..., 3)
+    deg: tuple
+    bnd: object
+    ext: int
+    extra: dict
+
+
+def config1(seed: int = 1) -> Workload:
+    """64^3, degree 1, circulant, ext = 0; FWHM-8 field scaled to +-2 vox."""
+    d = (64, 64, 64)
+    return Workload("pull+push 64^3 trilinear circulant ext=0", image(d, seed), deformation(d, seed + 1, 8.0, 2.0),
+                    (1, 1, 1), 0, 0, {})
+
+
+def config2(seed: int = 2) -> Workload:
+    """192^3, degree 3, DCT-II, ext = 1; FWHM-12 field scaled to +-5 vox; 1 channel."""
+    d = (192, 192, 192)
+    return Workload("pull+push 192^3 cubic DCT2 ext=1", image(d, seed), deformation(d, seed + 1, 12.0, 5.0),
+                    (3, 3, 3), 1, 1, {})
+
+
+def config3(seed: int = 3) -> Workload:
+    """160x192x160, degree 2, bounds (circulant, DCT-II, DST-II); target g = pull(f, phi2)."""
+    d = (160, 192, 160)
+    w = Workload("fused step 160x192x160 quadratic mixed bounds", image(d, seed),
+                 deformation(d, seed + 1, 12.0, 3.0), (2, 2, 2), (0, 1, 2), 1, {})
+    w.extra["phi2"] = deformation(d, seed + 2, 12.0, 3.0)
+    return w
+
+
+def config5(seed: int = 5) -> Workload:
+    """256^3 x 3 channels, degree 3, DCT-II; 0.25x contraction about the centre + field +-3 vox."""
+    d = (256, 256, 256)
+    return Workload("push 256^3x3 cubic DCT2 contraction", image(d, seed, channels=3),
+                    deformation(d, seed + 1, 12.0, 3.0, contraction=0.25), (3, 3, 3), 1, 1, {})
+
+
+def batched_pairs(seed: int = 4, npairs: int = 32, levels: int = 3):
+    """Uneven batch: sizes uniform in [64,256]x[64,256]x[64,192], 1-3 channels,
+    degree from {1,2,3}; each pair with a pyramid of ``levels`` (each level halved)."""
+    rng = np.random.default_rng(seed)
+    items = []
+    for p in range(npairs):
+        d = (int(rng.integers(64, 257)), int(rng.integers(64, 257)), int(rng.integers(64, 193)))
+        c = int(rng.integers(1, 4))
+        deg = int(rng.choice([1, 2, 3]))
+        for lev in range(levels):
+            dl = tuple(max(1, (v + (1 << lev) - 1) >> lev) for v in d)
+            items.append(dict(pair=p, level=lev, d=dl, channels=c, deg=deg, seed=seed * 1000 + p * 10 + lev))
+    return items

@@ -1,0 +1,67 @@
+"""Properties of the FP64 oracle that the reference's own tests check
+(test/runtests.jl:34-96): gradients against central finite differences and the
+push/pull adjoint identity, plus the same identity for pull_grad / push_grad."""
+from __future__ import annotations
+
+import itertools
+
+import numpy as np
+import pytest
+
+
+def _inputs(O, rng, d=(8, 7, 1), c=2, b=None, sigma=1.0):
+    shape_f = d + (c,) + ((b,) if b else ())
+    f1 = np.asfortranarray(rng.standard_normal(shape_f).astype(np.float32))
+    f2 = np.asfortranarray(rng.standard_normal(shape_f).astype(np.float32))
+    if b:
+        phi = np.stack([O.identity(d) + sigma * rng.standard_normal(d + (3,)).astype(np.float32)
+                        for _ in range(b)], axis=-1)
+    else:
+        phi = O.identity(d) + sigma * rng.standard_normal(d + (3,)).astype(np.float32)
+    return f1, f2, np.asfortranarray(phi.astype(np.float32))
+
+
+@pytest.mark.parametrize("deg,bnd,ext", list(itertools.product(range(5), [0, 1, 2, (0, 1, 2)], [0, 1])))
+def test_adjoint_identity(O, deg, bnd, ext):
+    """|<f1, pull(f2)> - <push(f1), f2>| small; the reference uses 1e-5 absolute (test/runtests.jl:93-95)."""
+    rng = np.random.default_rng(100 + deg)
+    s = O.Sett.make(deg, bnd, ext)
+    f1, f2, phi = _inputs(O, rng, d=(9, 7, 5), c=2, sigma=1.5)
+    lhs = np.nansum(f1.astype(np.float64) * O.pull(f2, phi, s))
+    rhs = np.sum(O.push(f1, phi, f2.shape[:3], s) * f2)
+    assert abs(lhs - rhs) <= 1e-10 * max(1.0, abs(lhs))
+    g = np.asfortranarray(rng.standard_normal((9, 7, 5, 3, 2)).astype(np.float32))
+    lhs = np.nansum(g.astype(np.float64) * O.pull_grad(f2, phi, s))
+    rhs = np.sum(O.push_grad(g, phi, f2.shape[:3], s) * f2)
+    assert abs(lhs - rhs) <= 1e-10 * max(1.0, abs(lhs))
+
+
+def _fd_phi_pull(O, f1, f2, phi, s):
+    """d/dphi of sum((pull(f1,phi)-f2)^2) by central differences (eps 0.01, test/utils.jl:7)."""
+    g = np.zeros(phi.shape)
+    p = phi.copy(order="F")
+    for idx in np.ndindex(phi.shape):
+        x0 = p[idx]
+        p[idx] = np.float32(x0 + np.float32(0.01))
+        hp = float(p[idx]) - float(x0)
+        ep = np.nansum((O.pull(f1, p, s) - f2) ** 2)
+        p[idx] = np.float32(x0 - np.float32(0.01))
+        hm = float(x0) - float(p[idx])
+        em = np.nansum((O.pull(f1, p, s) - f2) ** 2)
+        p[idx] = x0
+        g[idx] = (ep - em) / (hp + hm)
+    return g
+
+
+@pytest.mark.parametrize("deg", [2, 3])
+def test_fd_gradient_wrt_phi(O, deg):
+    """Analytic d/dphi (the pull rrule: sum_c delta * pull_grad, src/pushpull_pb.jl:11-18)
+    against central differences; relative squared error below 1e-3 as in test/runtests.jl:63-73."""
+    rng = np.random.default_rng(7 + deg)
+    s = O.Sett.make(deg, (0, 1, 2), 1)
+    f1, f2, phi = _inputs(O, rng)
+    r = O.pull(f1, phi, s) - f2                              # (d, C)
+    gr = O.pull_grad(f1, phi, s)                              # (d, 3, C)
+    ana = np.einsum("xyzc,xyzkc->xyzk", 2 * r, gr)
+    fd = _fd_phi_pull(O, f1, f2, phi, s)
+    assert np.sum((ana - fd) ** 2) / np.sum(ana ** 2) < 1e-3
