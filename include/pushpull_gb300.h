@@ -97,8 +97,31 @@ int pp_push_grad(float *g0, const float *phi, const float *g1,
                  const int *bnd, int nbnd, const int deg[3], int ext,
                  int accumulate, void *stream);
 
+/* ---- kernel selection ------------------------------------------------- */
+/* Ops for the tile registry. */
+enum pp_op { PP_OP_PULL = 0, PP_OP_PULL_GRAD = 1, PP_OP_PULL_HESS = 2, PP_OP_PUSH = 3, PP_OP_PUSH_GRAD = 4 };
+/* PP_PATH_AUTO: shared-memory tiled kernels where the degree is isotropic,
+ * per-voxel global-memory kernels otherwise; PP_PATH_DIRECT: always the latter. */
+enum pp_path { PP_PATH_AUTO = 0, PP_PATH_DIRECT = 1 };
+
+/* Tile of sample voxels per CTA (2^lx x 2^ly x 2^lz, 32..512 voxels) and the
+ * shared-memory budget of its image footprint box in floats, for one op
+ * (-1: all ops) and one isotropic degree (-1: all degrees).  No reference
+ * counterpart (the reference launches one thread per voxel with no tiling,
+ * ext/pushpull_gpu.jl:386-391); used by the autotuner. */
+int pp_set_tile(int op, int deg, int lx, int ly, int lz, int cap_floats);
+int pp_get_tile(int op, int deg, int *lx, int *ly, int *lz, int *cap_floats);
+/* Kernel family choice for all later calls in the process (PP_PATH_*). */
+int pp_set_path(int path);
+
 /* Message of the last failing call on this thread ("" when none). */
 const char *pp_last_error(void);
+
+/* Device status word of the current device (bit 0: a bounded device-side wait
+ * gave up; such a kernel skips its remaining work and returns).  reset != 0
+ * clears it.  Returns 0xffffffff if it cannot be read.  No reference
+ * counterpart (the reference kernels never wait). */
+unsigned pp_device_status(int reset);
 
 /* Library version: major*10000 + minor*100 + patch. */
 int pp_version(void);

@@ -37,7 +37,11 @@ _SIGS = {
     "pp_push_grad": (C.c_int, [_vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int,
                                _i32x3, C.c_int, C.c_int, _vp]),
     "pp_last_error": (C.c_char_p, []),
+    "pp_set_tile": (C.c_int, [C.c_int] * 6),
+    "pp_get_tile": (C.c_int, [C.c_int, C.c_int] + [C.POINTER(C.c_int)] * 4),
+    "pp_set_path": (C.c_int, [C.c_int]),
     "pp_version": (C.c_int, []),
+    "pp_device_status": (C.c_uint, [C.c_int]),
     # compatibility layer: reference CPU signatures on host pointers
     "pull": (None, [_vp, _vp, _vp, _vp, C.c_ulonglong, _vp, _vp, C.c_int]),
     "pullg": (None, [_vp, _vp, _vp, _vp, C.c_ulonglong, _vp, _vp, C.c_int]),

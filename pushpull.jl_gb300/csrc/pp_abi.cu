@@ -8,6 +8,7 @@
 #include <string>
 
 #include "pp_kernels.cuh"
+#include "pp_tiled.cuh"
 #include "pushpull_gb300.h"
 
 namespace pp {
@@ -53,6 +54,33 @@ int sm_count() {
 
 void set_error_message(const char* msg) { g_err = msg ? msg : ""; }
 
+// ---- tile configuration registry (per op, per isotropic degree) and path choice
+namespace {
+std::mutex g_cfg_mu;
+TileCfg g_tiles[5][5];
+bool g_tiles_init = false;
+int g_path = PP_PATH_AUTO;
+
+void init_tiles_locked() {
+    if (g_tiles_init) return;
+    // 8x8x8 tiles; the push family keeps two words per accumulator element
+    for (int op = 0; op < 5; ++op)
+        for (int d = 0; d < 5; ++d) g_tiles[op][d] = TileCfg{3, 3, 3, op < 3 ? 8192 : 12288};
+    g_tiles_init = true;
+}
+}  // namespace
+
+TileCfg tile_for(int op_index, int deg) {
+    std::lock_guard<std::mutex> lk(g_cfg_mu);
+    init_tiles_locked();
+    return g_tiles[op_index][deg < 0 ? 0 : (deg > 4 ? 4 : deg)];
+}
+
+int current_path() {
+    std::lock_guard<std::mutex> lk(g_cfg_mu);
+    return g_path;
+}
+
 // Validate the common arguments and fill the launch descriptor.
 // comps_in / comps_out: planar components per channel of the input / output.
 static int prepare(LaunchArgs& a, float* out, const float* phi, const float* in,
@@ -87,6 +115,10 @@ static int prepare(LaunchArgs& a, float* out, const float* phi, const float* in,
     }
     if (!mul_ok(g.d0[0], g.d0[1], t) || !mul_ok(t, g.d0[2], g.n0)) return fail(PP_ERR_DIMS, "d0 overflows");
     if (!mul_ok(g.d1[0], g.d1[1], t) || !mul_ok(t, g.d1[2], g.n1)) return fail(PP_ERR_DIMS, "d1 overflows");
+    for (int k = 0; k < 3; ++k) {
+        volatile float dk = (float)g.d0[k];   // float arithmetic, as artifacts/C/pushpull.c:8-10
+        g.hi[k] = dk - 0.99f;
+    }
     g.nc = nc;
     g.nb = nb;
     g.ext = ext ? 1 : 0;
@@ -108,7 +140,12 @@ static int run_pull(int op, float* out, const float* phi, const float* f0, const
     LaunchArgs a{};
     int rc = prepare(a, out, phi, f0, d0, d1, nc, nb, bnd, nbnd, deg, ext);
     if (rc != PP_OK || a.g.n1 == 0) return rc;
-    cudaError_t e = launch_pull_direct(op, a, (cudaStream_t)stream);
+    const TileCfg t = tile_for(op, deg[0]);
+    cudaError_t e;
+    if (current_path() != PP_PATH_DIRECT && tiled_supported(a, t))
+        e = launch_pull_tiled(op, a, t, (cudaStream_t)stream);
+    else
+        e = launch_pull_direct(op, a, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "pull launch");
     return PP_OK;
 }
@@ -126,7 +163,12 @@ static int run_push(int op, float* out, const float* phi, const float* in, const
         if (e != cudaSuccess) return cuda_fail(e, "zero output");
     }
     if (g.n1 == 0) return PP_OK;
-    cudaError_t e = launch_push_direct(op, a, (cudaStream_t)stream);
+    const TileCfg t = tile_for(3 + op, deg[0]);
+    cudaError_t e;
+    if (current_path() != PP_PATH_DIRECT && tiled_supported(a, t))
+        e = launch_push_tiled(op, a, t, (cudaStream_t)stream);
+    else
+        e = launch_push_direct(op, a, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "push launch");
     return PP_OK;
 }
@@ -165,7 +207,43 @@ int pp_push_grad(float* g0, const float* phi, const float* g1, const pp_usize d0
 
 const char* pp_last_error(void) { return pp::g_err.c_str(); }
 
+int pp_set_tile(int op, int deg, int lx, int ly, int lz, int cap_floats) {
+    pp::g_err.clear();
+    if (op < -1 || op > 4) return pp::fail(PP_ERR_UNSUPPORTED, "op %d outside -1..4", op);
+    if (deg < -1 || deg > 4) return pp::fail(PP_ERR_DEGREE, "deg %d outside -1..4", deg);
+    if (lx < 0 || ly < 0 || lz < 0 || lx + ly + lz < 5 || lx + ly + lz > 9)
+        return pp::fail(PP_ERR_UNSUPPORTED, "tile 2^%d x 2^%d x 2^%d must hold 32..512 voxels", lx, ly, lz);
+    if (cap_floats < 64 || (cap_floats & 3) || cap_floats > (227 * 1024) / 4)
+        return pp::fail(PP_ERR_UNSUPPORTED, "cap %d floats must be a multiple of 4 in [64, 58112]", cap_floats);
+    std::lock_guard<std::mutex> lk(pp::g_cfg_mu);
+    pp::init_tiles_locked();
+    for (int o = 0; o < 5; ++o)
+        for (int d = 0; d < 5; ++d)
+            if ((op < 0 || o == op) && (deg < 0 || d == deg)) pp::g_tiles[o][d] = pp::TileCfg{lx, ly, lz, cap_floats};
+    return PP_OK;
+}
+
+int pp_get_tile(int op, int deg, int* lx, int* ly, int* lz, int* cap_floats) {
+    if (op < 0 || op > 4 || deg < 0 || deg > 4) return pp::fail(PP_ERR_UNSUPPORTED, "op/deg out of range");
+    if (!lx || !ly || !lz || !cap_floats) return pp::fail(PP_ERR_NULL, "outputs must not be NULL");
+    const pp::TileCfg t = pp::tile_for(op, deg);
+    *lx = t.lx;
+    *ly = t.ly;
+    *lz = t.lz;
+    *cap_floats = t.cap;
+    return PP_OK;
+}
+
+int pp_set_path(int path) {
+    if (path != PP_PATH_AUTO && path != PP_PATH_DIRECT) return pp::fail(PP_ERR_UNSUPPORTED, "path %d", path);
+    std::lock_guard<std::mutex> lk(pp::g_cfg_mu);
+    pp::g_path = path;
+    return PP_OK;
+}
+
 int pp_version(void) { return 100; }
+
+unsigned pp_device_status(int reset) { return pp::read_device_status(reset != 0); }
 
 }  // extern "C"
 

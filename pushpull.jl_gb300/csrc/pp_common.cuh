@@ -35,9 +35,30 @@ struct Geometry {
     int dp[3];           // degree + 1 per dimension
     int ext;             // extrapolate flag
     int nbnd;            // 1 or nc
+    float hi[3];         // (float)d0[k] - 0.99f: upper end of the ext == 0 band (float arithmetic)
 };
 
 __device__ __forceinline__ bool finitef(float v) { return fabsf(v) <= 3.402823466e38f; }
+
+// Explicit shared-memory accesses through 32-bit shared-window addresses, so
+// box reads and reductions are always issued as shared-space instructions.
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ float lds_f32(unsigned a) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ int lds_s32(unsigned a) {
+    int v;
+    asm volatile("ld.shared.s32 %0, [%1];" : "=r"(v) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ void red_shared_s32(unsigned a, int v) {
+    asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void red_shared_f32(unsigned a, float v) {
+    asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
 
 // x = phi - 1 and the validity test, exactly as the reference evaluates them.
 __device__ __forceinline__ bool load_valid(float p0, float p1, float p2, const Geometry& g,
@@ -47,10 +68,7 @@ __device__ __forceinline__ bool load_valid(float p0, float p1, float p2, const G
     x2 = __fsub_rn(p2, 1.0f);
     if (!(finitef(x0) && finitef(x1) && finitef(x2))) return false;
     if (g.ext) return true;
-    const float h0 = __fsub_rn(__ll2float_rn(g.d0[0]), 0.99f);
-    const float h1 = __fsub_rn(__ll2float_rn(g.d0[1]), 0.99f);
-    const float h2 = __fsub_rn(__ll2float_rn(g.d0[2]), 0.99f);
-    return x0 >= -0.01f && x0 <= h0 && x1 >= -0.01f && x1 <= h1 && x2 >= -0.01f && x2 <= h2;
+    return x0 >= -0.01f && x0 <= g.hi[0] && x1 >= -0.01f && x1 <= g.hi[1] && x2 >= -0.01f && x2 <= g.hi[2];
 }
 
 // Map an unbounded tap index into [0, d) and return the sign the boundary rule
@@ -77,12 +95,12 @@ __device__ __forceinline__ long long fold_tap(int bnd, long long i, long long d,
     return n2 - 1 - r;
 }
 
-// B-spline weights for the DP taps that start at the returned first tap.
-// ORD 0: values; 1: values and first derivative; 2: also the second derivative.
+// B-spline weights for the DP taps that start at the returned first tap (as a
+// float holding an integer).  ORD 0: values; 1: values and first derivative;
+// 2: also the second derivative.
 template <int DP, int ORD>
-__device__ __forceinline__ long long spline_taps(float x, float* w, float* dw, float* hw) {
+__device__ __forceinline__ float spline_weights(float x, float* w, float* dw, float* hw) {
     const float fo = ceilf(__fsub_rn(x, 0.5f * (float)DP));
-    const long long o = (long long)fo;
     if constexpr (DP == 1) {
         w[0] = 1.0f;
         if constexpr (ORD >= 1) dw[0] = 0.0f;
@@ -143,8 +161,23 @@ __device__ __forceinline__ long long spline_taps(float x, float* w, float* dw, f
             hw[3] = -2.5f + q * (5.0f - 2.0f * q);
         }
     }
-    return o;
+    return fo;
 }
+
+template <int DP, int ORD>
+__device__ __forceinline__ long long spline_taps(float x, float* w, float* dw, float* hw) {
+    return (long long)spline_weights<DP, ORD>(x, w, dw, hw);
+}
+
+// 32-bit first tap (saturating), for callers that know it is in range.
+template <int DP, int ORD>
+__device__ __forceinline__ int spline_taps32(float x, float* w, float* dw, float* hw) {
+    return __float2int_rz(spline_weights<DP, ORD>(x, w, dw, hw));
+}
+
+// First tap as a saturating 32-bit integer: ceil(x - dp/2) with the reference's
+// float rounding; equals (int64) ceilf(...) whenever that fits in 32 bits.
+__device__ __forceinline__ int first_tap32(float x, int DP) { return __float2int_ru(__fsub_rn(x, 0.5f * (float)DP)); }
 
 // Runtime-degree variant (dp in 1..5) writing kMaxDP slots; unused slots get 0.
 template <int ORD>

@@ -1,0 +1,35 @@
+// pp_tiled.cuh -- tile configuration and launchers of the shared-memory tiled kernels.
+#pragma once
+
+#include "pp_kernels.cuh"
+
+namespace pp {
+
+// Tile of sample voxels handled by one CTA: 2^lx x 2^ly x 2^lz (32..512 voxels),
+// and the shared-memory budget of its footprint box, in floats (multiple of 4).
+struct TileCfg {
+    int lx, ly, lz;
+    int cap;
+};
+
+bool tiled_supported(const LaunchArgs& a, const TileCfg& t);
+cudaError_t launch_pull_tiled(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s);
+cudaError_t launch_push_tiled(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s);
+
+// Geometry of the tile grid, computed on the host once per launch.
+struct TileGrid {
+    int lx, ly, lz;     // log2 tile sides
+    int ntx, nty, ntz;  // tiles per dimension
+    int ntiles;         // ntx * nty * ntz * nb (tiles of all batches)
+    // q = (u * m) >> s equals u / n{x,y,z} for every u < 2^31 (multiply-shift division)
+    unsigned long long mx, my, mz;
+    int sx, sy, sz;
+    int cap;            // box budget in floats
+    int pmod;           // box row pitch P is chosen with P % 32 == pmod
+};
+
+// Read (and optionally clear) the device status word of the current device:
+// bit 0 = a bounded device-side wait gave up.  0xffffffff if it cannot be read.
+unsigned read_device_status(bool reset);
+
+}  // namespace pp
