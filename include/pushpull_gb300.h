@@ -78,6 +78,23 @@ int pp_pull_hess(float *h1, const float *phi, const float *f0,
                  const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
                  const int *bnd, int nbnd, const int deg[3], int ext, void *stream);
 
+/* dphi = sum_c up_c * grad pull(f0_c, phi), written as (d1[0], d1[1], d1[2], 3, nb):
+ * the deformation cotangent of pull (rrule, src/pushpull_pb.jl:15-17: sum over
+ * channels of delta .* pull_grad) and of push (:508-510 with up = f1 and f0 =
+ * delta), computed without the (d1, 3, nc, nb) pull_grad temporary.
+ * up has the layout of a pull output, (d1, nc, nb).  Invalid voxels get NaN. */
+int pp_pull_grad_dot(float *dphi, const float *phi, const float *f0, const float *up,
+                     const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
+                     const int *bnd, int nbnd, const int deg[3], int ext, void *stream);
+
+/* dphi[p] = sum_c sum_q H_c[p,q] up_c[q], H_c the Hessian of pull(f0_c, phi):
+ * the deformation cotangent of pull_grad (rrule, src/pushpull_pb.jl:26-35,
+ * sum over channels and q of delta .* pull_hess).  up has the layout of a
+ * pull_grad output, (d1, 3, nc, nb); dphi is (d1, 3, nb). */
+int pp_pull_hess_dot(float *dphi, const float *phi, const float *f0, const float *up,
+                     const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
+                     const int *bnd, int nbnd, const int deg[3], int ext, void *stream);
+
 /* f0 (+)= push(f1, phi): replaces push (src/pushpull_cpu.jl:165-203,
  * ext/pushpull_gpu.jl:165-201; push, pushpull.c:147-164).  accumulate != 0 adds
  * into the caller's f0 (the reference contract: the caller zero-fills);
@@ -97,9 +114,59 @@ int pp_push_grad(float *g0, const float *phi, const float *g1,
                  const int *bnd, int nbnd, const int deg[3], int ext,
                  int accumulate, void *stream);
 
+/* Fused forward + adjoint step of the loss sum((pull(f0, phi) - g)^2):
+ *   *loss (device double) = sum over batch, channel and voxel of r^2, r = pull(f0, phi) - g
+ *   df   (d0, nc, nb)  (+)= push(2 r, phi)               -- the f0 cotangent
+ *   dphi (d1, 3, nb)     = sum_c 2 r_c grad pull(f0_c)    -- the phi cotangent
+ * in one pass over phi, f0 and g.  Replaces the reference's differentiable
+ * step built from pull, the pull rrule (src/pushpull_pb.jl:11-18: push and
+ * pull_grad) and two broadcasts.  g has the layout of a pull output, (d1, nc, nb).
+ * Invalid voxels make the loss NaN and their dphi NaN; non-finite residuals are
+ * not pushed.  accumulate applies to df only.  The loss is reduced in a fixed
+ * order and is reproducible from run to run.  Uses stream-ordered scratch (one
+ * double per CTA, one float per image volume) from a memory pool this library
+ * owns per device. */
+int pp_fused_step(double *loss, float *df, float *dphi, const float *f0, const float *phi, const float *g,
+                  const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
+                  const int *bnd, int nbnd, const int deg[3], int ext, int accumulate, void *stream);
+
+/* ---- batched uneven workload ------------------------------------------- */
+/* One (image, deformation) pair of a batch: f1 = pull(f0, phi) is written and
+ * out (+)= push(f1, phi) is accumulated, all device pointers, single batch,
+ * isotropic degree.  Items may differ in size, channels, degree and bounds
+ * (e.g. registration pairs and their multigrid pyramid levels). */
+typedef struct {
+    const float *f0;      /* (d0, nc)     */
+    const float *phi;     /* (d1, 3)      */
+    float *f1;            /* (d1, nc)     */
+    float *out;           /* (d0, nc)     */
+    pp_usize d0[3], d1[3];
+    int nc, deg;          /* channels, isotropic degree 0..4 */
+    int bnd[3], ext;      /* boundary codes (all channels), extrapolate */
+} pp_batch_item;
+
+typedef struct pp_batch pp_batch;
+
+/* Build a plan: item descriptors go to device memory once.  zero_outputs != 0
+ * zeroes every out before each run.  No reference counterpart: the reference
+ * loops over arrays and levels on the host (ext/pushpull_gpu.jl:37-49,
+ * src/multigrid.jl:21-55). */
+int pp_batch_create(pp_batch **plan, const pp_batch_item *items, int n, int zero_outputs);
+/* Total tiles of the plan (the unit of work of its persistent launch). */
+int pp_batch_tiles(const pp_batch *plan);
+/* Run the plan: every tile of every item in one persistent launch (tiles are
+ * claimed from a device work counter, balancing uneven items). */
+int pp_batch_run(pp_batch *plan, void *stream);
+/* Capture one run into a CUDA graph held by the plan (runs it once eagerly
+ * first); pp_batch_launch replays the graph. */
+int pp_batch_capture(pp_batch *plan, void *stream);
+int pp_batch_launch(pp_batch *plan, void *stream);
+void pp_batch_destroy(pp_batch *plan);
+
 /* ---- kernel selection ------------------------------------------------- */
 /* Ops for the tile registry. */
-enum pp_op { PP_OP_PULL = 0, PP_OP_PULL_GRAD = 1, PP_OP_PULL_HESS = 2, PP_OP_PUSH = 3, PP_OP_PUSH_GRAD = 4 };
+enum pp_op { PP_OP_PULL = 0, PP_OP_PULL_GRAD = 1, PP_OP_PULL_HESS = 2, PP_OP_PUSH = 3, PP_OP_PUSH_GRAD = 4,
+             PP_OP_FUSED = 5 };
 /* PP_PATH_AUTO: shared-memory tiled kernels where the degree is isotropic,
  * per-voxel global-memory kernels otherwise; PP_PATH_DIRECT: always the latter. */
 enum pp_path { PP_PATH_AUTO = 0, PP_PATH_DIRECT = 1 };
@@ -111,6 +178,16 @@ enum pp_path { PP_PATH_AUTO = 0, PP_PATH_DIRECT = 1 };
  * ext/pushpull_gpu.jl:386-391); used by the autotuner. */
 int pp_set_tile(int op, int deg, int lx, int ly, int lz, int cap_floats);
 int pp_get_tile(int op, int deg, int *lx, int *ly, int *lz, int *cap_floats);
+/* Autotuner: times the per-voxel kernels and every candidate tile shape and
+ * shared-memory budget for op (PP_OP_PULL .. PP_OP_PUSH_GRAD) on the caller's
+ * own arguments (same meaning as the op's entry point; push ops run with
+ * accumulate = 0, so out is overwritten), reps timed runs each with CUDA
+ * events, installs the best tiled configuration for (op, deg[0]) and returns
+ * best = {lx, ly, lz, cap, path} (path PP_PATH_DIRECT when the per-voxel
+ * kernels were fastest) and its mean time in ms.  Synchronises the stream. */
+int pp_autotune(int op, float *out, const float *phi, const float *in, const pp_usize d0[3], const pp_usize d1[3],
+                int nc, int nb, const int *bnd, int nbnd, const int deg[3], int ext, int reps, void *stream,
+                int *best, float *best_ms);
 /* Kernel family choice for all later calls in the process (PP_PATH_*). */
 int pp_set_path(int path);
 

@@ -3,12 +3,14 @@
 Host-side mirror of the reference API (src/PushPull.jl:19-20 exports) over the
 C ABI of ``lib/libpushpull_gb300.so`` (include/pushpull_gb300.h).
 """
-from . import layout
+from . import autograd, layout
 from ._native import PushPullError, lib as native_library
-from .api import id, pull, pull_grad, pull_hess, push, push_grad
+from .api import (fused_step, id, pull, pull_grad, pull_grad_dot, pull_hess, pull_hess_dot, push,
+                  push_grad)
 from .settings import Settings, sett_chan
 
 __all__ = [
     "Settings", "sett_chan", "pull", "pull_grad", "pull_hess", "push", "push_grad", "id",
-    "layout", "PushPullError", "native_library",
+    "pull_grad_dot", "pull_hess_dot", "fused_step", "autograd", "layout", "PushPullError",
+    "native_library",
 ]

@@ -24,6 +24,13 @@ _u64x3 = C.c_ulonglong * 3
 _i32x3 = C.c_int * 3
 _vp = C.c_void_p
 
+class BatchItem(C.Structure):
+    """pp_batch_item of include/pushpull_gb300.h."""
+    _fields_ = [("f0", _vp), ("phi", _vp), ("f1", _vp), ("out", _vp), ("d0", C.c_ulonglong * 3),
+                ("d1", C.c_ulonglong * 3), ("nc", C.c_int), ("deg", C.c_int), ("bnd", C.c_int * 3),
+                ("ext", C.c_int)]
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "pp_pull": (C.c_int, [_vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int, _i32x3,
@@ -32,10 +39,24 @@ _SIGS = {
                                _i32x3, C.c_int, _vp]),
     "pp_pull_hess": (C.c_int, [_vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int,
                                _i32x3, C.c_int, _vp]),
+    "pp_pull_grad_dot": (C.c_int, [_vp, _vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int,
+                                   _i32x3, C.c_int, _vp]),
+    "pp_pull_hess_dot": (C.c_int, [_vp, _vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int,
+                                   _i32x3, C.c_int, _vp]),
     "pp_push": (C.c_int, [_vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int, _i32x3,
                           C.c_int, C.c_int, _vp]),
     "pp_push_grad": (C.c_int, [_vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int,
                                _i32x3, C.c_int, C.c_int, _vp]),
+    "pp_fused_step": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int,
+                                _i32x3, C.c_int, C.c_int, _vp]),
+    "pp_batch_create": (C.c_int, [C.POINTER(_vp), C.POINTER(BatchItem), C.c_int, C.c_int]),
+    "pp_batch_tiles": (C.c_int, [_vp]),
+    "pp_batch_run": (C.c_int, [_vp, _vp]),
+    "pp_batch_capture": (C.c_int, [_vp, _vp]),
+    "pp_batch_launch": (C.c_int, [_vp, _vp]),
+    "pp_batch_destroy": (None, [_vp]),
+    "pp_autotune": (C.c_int, [C.c_int, _vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int, _i32x3,
+                              C.c_int, C.c_int, _vp, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "pp_last_error": (C.c_char_p, []),
     "pp_set_tile": (C.c_int, [C.c_int] * 6),
     "pp_get_tile": (C.c_int, [C.c_int, C.c_int] + [C.POINTER(C.c_int)] * 4),

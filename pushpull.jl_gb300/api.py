@@ -147,3 +147,69 @@ def id(v: torch.Tensor = None, *, affine=None, dim=None, device=None) -> torch.T
             phi[..., k] = (A[k][0] * x.double() + A[k][1] * y.double() + A[k][2] * z.double()
                            + A[k][3]).float()
     return phi
+
+
+def _dot_family(fn: str, f0, phi, up, sett: Settings, up_comps: int):
+    assert 3 <= f0.dim() <= 5, "`f₀` must have between 3 & 5 dimensions"
+    assert 4 <= phi.dim() <= 5, "`ϕ` must have 4 or 5 dimensions"
+    assert L.jsize(phi, 4) == 3, "`ϕ` must have three channels"
+    assert L.jsize(phi, 5) == L.jsize(f0, 5), "`ϕ` & `f₀` must have the same batch size"
+    nc, nb = L.jsize(f0, 4), L.jsize(f0, 5)
+    assert len(sett.bnd) == nc or len(sett.bnd) == 1
+    d1 = tuple(phi.shape[:3])
+    want = d1 + ((3,) if up_comps == 3 else ()) + (nc, nb)
+    assert up.numel() == int(torch.tensor(want).prod()), "upstream does not match the sample grid"
+    _require_cuda(f0, phi, up)
+    f0, phi, up = L.colmajor(f0), L.colmajor(phi), L.colmajor(up)
+    out = L.empty(tuple(phi.shape), device=f0.device)
+    lib = _native.lib()
+    rc = getattr(lib, fn)(out.data_ptr(), phi.data_ptr(), f0.data_ptr(), up.data_ptr(),
+                          _native.u64x3(f0.shape[:3]), _native.u64x3(d1), nc, nb, sett.bnd_array(), sett.nbnd,
+                          _native.i32x3(sett.deg), sett.ext, _stream(f0))
+    _native.check(fn, rc)
+    return out
+
+
+def pull_grad_dot(f0: torch.Tensor, phi: torch.Tensor, up: torch.Tensor, sett: Settings = Settings()) -> torch.Tensor:
+    """``Σ_c up_c · ∇pull(f₀_c, ϕ)`` with the shape of ``ϕ``: the ϕ-cotangent of ``pull``
+    (src/pushpull_pb.jl:11-18) without the ``(d₁…, 3, C, B)`` temporary."""
+    return _dot_family("pp_pull_grad_dot", f0, phi, up, sett, 1)
+
+
+def pull_hess_dot(f0: torch.Tensor, phi: torch.Tensor, up: torch.Tensor, sett: Settings = Settings()) -> torch.Tensor:
+    """``Σ_c H_c · up_c`` with the shape of ``ϕ``: the ϕ-cotangent of ``pull_grad``
+    (src/pushpull_pb.jl:26-35); ``up`` has the shape of a ``pull_grad`` output."""
+    return _dot_family("pp_pull_hess_dot", f0, phi, up, sett, 3)
+
+
+def fused_step(f0: torch.Tensor, phi: torch.Tensor, g: torch.Tensor, sett: Settings = Settings(), *,
+               df_out=None, accumulate: bool = False):
+    """Loss ``Σ (pull(f₀, ϕ) - g)²`` and its gradients in one pass.
+
+    Returns ``(loss, df, dphi)``: ``loss`` a 0-d float64 CUDA tensor, ``df`` with the
+    shape of ``f₀`` (= push(2r)), ``dphi`` with the shape of ``ϕ`` (= Σ_c 2r_c ∇pull_c)."""
+    assert 3 <= f0.dim() <= 5 and 4 <= phi.dim() <= 5 and L.jsize(phi, 4) == 3
+    assert L.jsize(phi, 5) == L.jsize(f0, 5), "`ϕ` & `f₀` must have the same batch size"
+    nc, nb = L.jsize(f0, 4), L.jsize(f0, 5)
+    assert len(sett.bnd) == nc or len(sett.bnd) == 1
+    d1 = tuple(phi.shape[:3])
+    assert tuple(g.shape[:3]) == d1 and g.numel() == int(torch.tensor(d1).prod()) * nc * nb, \
+        "`g` must have the shape of pull(f₀, ϕ)"
+    _require_cuda(f0, phi, g)
+    f0, phi, g = L.colmajor(f0), L.colmajor(phi), L.colmajor(g)
+    if df_out is None:
+        df = L.empty(tuple(f0.shape), device=f0.device)
+        accumulate = False
+    else:
+        _require_cuda(df_out)
+        assert tuple(df_out.shape) == tuple(f0.shape) and L.is_colmajor(df_out)
+        df = df_out
+    dphi = L.empty(tuple(phi.shape), device=f0.device)
+    loss = torch.empty((), dtype=torch.float64, device=f0.device)
+    lib = _native.lib()
+    rc = lib.pp_fused_step(loss.data_ptr(), df.data_ptr(), dphi.data_ptr(), f0.data_ptr(), phi.data_ptr(),
+                           g.data_ptr(), _native.u64x3(f0.shape[:3]), _native.u64x3(d1), nc, nb,
+                           sett.bnd_array(), sett.nbnd, _native.i32x3(sett.deg), sett.ext, int(bool(accumulate)),
+                           _stream(f0))
+    _native.check("pp_fused_step", rc)
+    return loss, df, dphi

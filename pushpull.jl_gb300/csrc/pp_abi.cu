@@ -54,18 +54,51 @@ int sm_count() {
 
 void set_error_message(const char* msg) { g_err = msg ? msg : ""; }
 
+// Stream-ordered scratch comes from a memory pool owned by this library, one per
+// device, that keeps its memory between calls (the device's default pool returns
+// memory to the system at every synchronisation, which would re-map it per call).
+static cudaError_t scratch_pool(cudaMemPool_t* out) {
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!pools[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t p;
+        if ((e = cudaMemPoolCreate(&p, &props)) != cudaSuccess) return e;
+        unsigned long long keep = ~0ULL;
+        if ((e = cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess) return e;
+        pools[dev] = p;
+    }
+    *out = pools[dev];
+    return cudaSuccess;
+}
+
+cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
+    cudaMemPool_t pool;
+    cudaError_t e = scratch_pool(&pool);
+    if (e != cudaSuccess) return e;
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+
 // ---- tile configuration registry (per op, per isotropic degree) and path choice
 namespace {
 std::mutex g_cfg_mu;
-TileCfg g_tiles[5][5];
+TileCfg g_tiles[6][5];   // ops: pull, pull_grad, pull_hess, push, push_grad, fused step
 bool g_tiles_init = false;
 int g_path = PP_PATH_AUTO;
 
 void init_tiles_locked() {
     if (g_tiles_init) return;
     // 8x8x8 tiles; the push family keeps two words per accumulator element
-    for (int op = 0; op < 5; ++op)
-        for (int d = 0; d < 5; ++d) g_tiles[op][d] = TileCfg{3, 3, 3, op < 3 ? 8192 : 12288};
+    for (int op = 0; op < 6; ++op)
+        for (int d = 0; d < 5; ++d) g_tiles[op][d] = TileCfg{3, 3, 3, op < 3 ? 8192 : (op < 5 ? 16384 : 4096)};
     g_tiles_init = true;
 }
 }  // namespace
@@ -134,13 +167,33 @@ static int prepare(LaunchArgs& a, float* out, const float* phi, const float* in,
     return PP_OK;
 }
 
+int fail_status(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+int prepare_args(LaunchArgs& a, float* out, const float* phi, const float* in, const pp_usize d0[3],
+                 const pp_usize d1[3], int nc, int nb, const int* bnd, int nbnd, const int deg[3], int ext) {
+    return prepare(a, out, phi, in, d0, d1, nc, nb, bnd, nbnd, deg, ext);
+}
+
 static int run_pull(int op, float* out, const float* phi, const float* f0, const pp_usize d0[3],
                     const pp_usize d1[3], int nc, int nb, const int* bnd, int nbnd, const int deg[3],
-                    int ext, void* stream) {
+                    int ext, void* stream, const float* up = nullptr) {
     LaunchArgs a{};
     int rc = prepare(a, out, phi, f0, d0, d1, nc, nb, bnd, nbnd, deg, ext);
     if (rc != PP_OK || a.g.n1 == 0) return rc;
-    const TileCfg t = tile_for(op, deg[0]);
+    if (op == kPullGradDot || op == kPullHessDot) {
+        if (!up) return fail(PP_ERR_NULL, "upstream pointer must not be NULL");
+        if (!aligned4(up)) return fail(PP_ERR_ALIGN, "float pointers must be 4-byte aligned");
+        a.up = up;
+    }
+    const TileCfg t = tile_for(op < 3 ? op : op - 2, deg[0]);
     cudaError_t e;
     if (current_path() != PP_PATH_DIRECT && tiled_supported(a, t))
         e = launch_pull_tiled(op, a, t, (cudaStream_t)stream);
@@ -173,8 +226,63 @@ static int run_push(int op, float* out, const float* phi, const float* in, const
     return PP_OK;
 }
 
+// Fused step: loss (double, written), df (accumulated or zeroed first), dphi (written).
+static int run_fused(double* loss, float* df, float* dphi, const float* f0, const float* phi, const float* g,
+                     const pp_usize d0[3], const pp_usize d1[3], int nc, int nb, const int* bnd, int nbnd,
+                     const int deg[3], int ext, int accumulate, void* stream) {
+    LaunchArgs a{};
+    int rc = prepare(a, df, phi, f0, d0, d1, nc, nb, bnd, nbnd, deg, ext);
+    if (rc != PP_OK) return rc;
+    if (!loss) return fail(PP_ERR_NULL, "loss pointer must not be NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e;
+    if (!accumulate && a.g.n0 > 0 && df) {
+        e = cudaMemsetAsync(df, 0, (size_t)a.g.n0 * a.g.nc * a.g.nb * sizeof(float), s);
+        if (e != cudaSuccess) return cuda_fail(e, "zero df");
+    }
+    if (a.g.n1 == 0) {
+        e = cudaMemsetAsync(loss, 0, sizeof(double), s);
+        return e == cudaSuccess ? PP_OK : cuda_fail(e, "zero loss");
+    }
+    if (!g || !dphi) return fail(PP_ERR_NULL, "g and dphi must not be NULL");
+    if (!aligned4(g) || !aligned4(dphi)) return fail(PP_ERR_ALIGN, "float pointers must be 4-byte aligned");
+    a.up = g;
+    a.out2 = dphi;
+    const TileCfg t = tile_for(PP_OP_FUSED, deg[0]);
+    const bool tiled = current_path() != PP_PATH_DIRECT && tiled_supported(a, t);
+    long long slots;
+    int grid = 0;
+    if (tiled) {
+        grid = fused_tiled_grid(a, t);
+        slots = grid;
+    } else {
+        const dim3 gd = fused_direct_grid(a);
+        slots = (long long)gd.x * gd.y;
+    }
+    // scratch, stream ordered: per-CTA loss partials and max |f0| per (channel, batch)
+    const int planes = a.g.nc * a.g.nb;
+    const size_t part_bytes = ((size_t)slots * sizeof(double) + 255) & ~(size_t)255;
+    double* partial = nullptr;
+    e = scratch_alloc(reinterpret_cast<void**>(&partial), part_bytes + (size_t)planes * sizeof(unsigned), s);
+    if (e != cudaSuccess) return cuda_fail(e, "allocate scratch");
+    unsigned* fmax = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(partial) + part_bytes);
+    a.partial = partial;
+    a.fmax = fmax;
+    if (tiled) {
+        e = cudaMemsetAsync(fmax, 0, (size_t)planes * sizeof(unsigned), s);
+        if (e == cudaSuccess) e = launch_absmax(f0, a.g.n0, planes, fmax, s);
+    }
+    if (e == cudaSuccess) e = tiled ? launch_fused_tiled(a, t, s, grid) : launch_fused_direct(a, s);
+    if (e == cudaSuccess) e = launch_sum_partials(partial, (int)slots, loss, s);
+    const cudaError_t ef = cudaFreeAsync(partial, s);
+    if (e != cudaSuccess) return cuda_fail(e, "fused step launch");
+    if (ef != cudaSuccess) return cuda_fail(ef, "free loss partials");
+    return PP_OK;
+}
+
 }  // namespace pp
 
+using pp::run_fused;
 using pp::run_pull;
 using pp::run_push;
 
@@ -195,6 +303,18 @@ int pp_pull_hess(float* h1, const float* phi, const float* f0, const pp_usize d0
     return run_pull(pp::kPullHess, h1, phi, f0, d0, d1, nc, nb, bnd, nbnd, deg, ext, stream);
 }
 
+int pp_pull_grad_dot(float* dphi, const float* phi, const float* f0, const float* up, const pp_usize d0[3],
+                     const pp_usize d1[3], int nc, int nb, const int* bnd, int nbnd, const int deg[3], int ext,
+                     void* stream) {
+    return run_pull(pp::kPullGradDot, dphi, phi, f0, d0, d1, nc, nb, bnd, nbnd, deg, ext, stream, up);
+}
+
+int pp_pull_hess_dot(float* dphi, const float* phi, const float* f0, const float* up, const pp_usize d0[3],
+                     const pp_usize d1[3], int nc, int nb, const int* bnd, int nbnd, const int deg[3], int ext,
+                     void* stream) {
+    return run_pull(pp::kPullHessDot, dphi, phi, f0, d0, d1, nc, nb, bnd, nbnd, deg, ext, stream, up);
+}
+
 int pp_push(float* f0, const float* phi, const float* f1, const pp_usize d0[3], const pp_usize d1[3], int nc,
             int nb, const int* bnd, int nbnd, const int deg[3], int ext, int accumulate, void* stream) {
     return run_push(pp::kPush, f0, phi, f1, d0, d1, nc, nb, bnd, nbnd, deg, ext, accumulate, stream);
@@ -205,11 +325,17 @@ int pp_push_grad(float* g0, const float* phi, const float* g1, const pp_usize d0
     return run_push(pp::kPushGrad, g0, phi, g1, d0, d1, nc, nb, bnd, nbnd, deg, ext, accumulate, stream);
 }
 
+int pp_fused_step(double* loss, float* df, float* dphi, const float* f0, const float* phi, const float* g,
+                  const pp_usize d0[3], const pp_usize d1[3], int nc, int nb, const int* bnd, int nbnd,
+                  const int deg[3], int ext, int accumulate, void* stream) {
+    return run_fused(loss, df, dphi, f0, phi, g, d0, d1, nc, nb, bnd, nbnd, deg, ext, accumulate, stream);
+}
+
 const char* pp_last_error(void) { return pp::g_err.c_str(); }
 
 int pp_set_tile(int op, int deg, int lx, int ly, int lz, int cap_floats) {
     pp::g_err.clear();
-    if (op < -1 || op > 4) return pp::fail(PP_ERR_UNSUPPORTED, "op %d outside -1..4", op);
+    if (op < -1 || op > 5) return pp::fail(PP_ERR_UNSUPPORTED, "op %d outside -1..5", op);
     if (deg < -1 || deg > 4) return pp::fail(PP_ERR_DEGREE, "deg %d outside -1..4", deg);
     if (lx < 0 || ly < 0 || lz < 0 || lx + ly + lz < 5 || lx + ly + lz > 9)
         return pp::fail(PP_ERR_UNSUPPORTED, "tile 2^%d x 2^%d x 2^%d must hold 32..512 voxels", lx, ly, lz);
@@ -217,14 +343,14 @@ int pp_set_tile(int op, int deg, int lx, int ly, int lz, int cap_floats) {
         return pp::fail(PP_ERR_UNSUPPORTED, "cap %d floats must be a multiple of 4 in [64, 58112]", cap_floats);
     std::lock_guard<std::mutex> lk(pp::g_cfg_mu);
     pp::init_tiles_locked();
-    for (int o = 0; o < 5; ++o)
+    for (int o = 0; o < 6; ++o)
         for (int d = 0; d < 5; ++d)
             if ((op < 0 || o == op) && (deg < 0 || d == deg)) pp::g_tiles[o][d] = pp::TileCfg{lx, ly, lz, cap_floats};
     return PP_OK;
 }
 
 int pp_get_tile(int op, int deg, int* lx, int* ly, int* lz, int* cap_floats) {
-    if (op < 0 || op > 4 || deg < 0 || deg > 4) return pp::fail(PP_ERR_UNSUPPORTED, "op/deg out of range");
+    if (op < 0 || op > 5 || deg < 0 || deg > 4) return pp::fail(PP_ERR_UNSUPPORTED, "op/deg out of range");
     if (!lx || !ly || !lz || !cap_floats) return pp::fail(PP_ERR_NULL, "outputs must not be NULL");
     const pp::TileCfg t = pp::tile_for(op, deg);
     *lx = t.lx;
@@ -242,6 +368,93 @@ int pp_set_path(int path) {
 }
 
 int pp_version(void) { return 100; }
+
+int pp_autotune(int op, float* out, const float* phi, const float* in, const pp_usize d0[3], const pp_usize d1[3],
+                int nc, int nb, const int* bnd, int nbnd, const int deg[3], int ext, int reps, void* stream,
+                int* best, float* best_ms) {
+    using namespace pp;
+    if (op < 0 || op > 4) return fail(PP_ERR_UNSUPPORTED, "autotune supports ops 0..4 (got %d)", op);
+    if (!deg || !best || !best_ms) return fail(PP_ERR_NULL, "deg, best and best_ms must not be NULL");
+    if (deg[0] < 0 || deg[0] > 4) return fail(PP_ERR_DEGREE, "deg[0] = %d outside 0..4", deg[0]);
+    if (reps < 1) reps = 3;
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool is_push = op >= 3;
+    auto run = [&]() -> int {
+        switch (op) {
+            case 0: return pp_pull(out, phi, in, d0, d1, nc, nb, bnd, nbnd, deg, ext, stream);
+            case 1: return pp_pull_grad(out, phi, in, d0, d1, nc, nb, bnd, nbnd, deg, ext, stream);
+            case 2: return pp_pull_hess(out, phi, in, d0, d1, nc, nb, bnd, nbnd, deg, ext, stream);
+            case 3: return pp_push(out, phi, in, d0, d1, nc, nb, bnd, nbnd, deg, ext, 0, stream);
+            default: return pp_push_grad(out, phi, in, d0, d1, nc, nb, bnd, nbnd, deg, ext, 0, stream);
+        }
+    };
+    const int tiles[][3] = {{3, 3, 3}, {4, 3, 2}, {4, 2, 3}, {5, 2, 2}, {3, 4, 2}, {3, 3, 2}, {4, 2, 2}};
+    const int caps_pull[] = {6144, 8192, 12288};
+    const int caps_push[] = {12288, 16384, 20480};
+    const TileCfg saved = tile_for(op, deg[0]);
+    const int saved_path = current_path();
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        return fail(PP_ERR_CUDA, "event create");
+    float bestv = 3.0e38f;
+    int bcfg[5] = {saved.lx, saved.ly, saved.lz, saved.cap, PP_PATH_AUTO};
+    auto measure = [&](float& ms) -> int {
+        int rc = run();                                   // warm-up (and one-time set-up)
+        if (rc != PP_OK) return rc;
+        float tot = 0.f;
+        for (int r = 0; r < reps; ++r) {
+            cudaEventRecord(e0, s);
+            rc = run();
+            cudaEventRecord(e1, s);
+            if (rc != PP_OK) return rc;
+            if (cudaEventSynchronize(e1) != cudaSuccess) return fail(PP_ERR_CUDA, "event sync");
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            tot += t;
+        }
+        ms = tot / reps;
+        return PP_OK;
+    };
+    int rc = PP_OK;
+    // the per-voxel kernels
+    pp_set_path(PP_PATH_DIRECT);
+    float ms = 0.f;
+    if ((rc = measure(ms)) == PP_OK && ms < bestv) {
+        bestv = ms;
+        bcfg[4] = PP_PATH_DIRECT;
+    }
+    pp_set_path(PP_PATH_AUTO);
+    for (const auto& t : tiles) {
+        for (int ci = 0; ci < 3 && rc == PP_OK; ++ci) {
+            const int cap = is_push ? caps_push[ci] : caps_pull[ci];
+            if (pp_set_tile(op, deg[0], t[0], t[1], t[2], cap) != PP_OK) continue;
+            if ((rc = measure(ms)) != PP_OK) break;
+            if (ms < bestv) {
+                bestv = ms;
+                bcfg[0] = t[0];
+                bcfg[1] = t[1];
+                bcfg[2] = t[2];
+                bcfg[3] = cap;
+                bcfg[4] = PP_PATH_AUTO;
+            }
+        }
+        if (rc != PP_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    pp_set_path(saved_path);
+    if (rc != PP_OK) {
+        pp_set_tile(op, deg[0], saved.lx, saved.ly, saved.lz, saved.cap);
+        return rc;
+    }
+    // the per-voxel path wins only in the registry's absence of a tiled choice:
+    // keep the tile configuration that was best among the tiled candidates
+    if (bcfg[4] == PP_PATH_AUTO) pp_set_tile(op, deg[0], bcfg[0], bcfg[1], bcfg[2], bcfg[3]);
+    else pp_set_tile(op, deg[0], saved.lx, saved.ly, saved.lz, saved.cap);
+    for (int k = 0; k < 5; ++k) best[k] = bcfg[k];
+    *best_ms = bestv;
+    return PP_OK;
+}
 
 unsigned pp_device_status(int reset) { return pp::read_device_status(reset != 0); }
 

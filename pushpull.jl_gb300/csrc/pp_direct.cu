@@ -81,8 +81,12 @@ cudaError_t launch_pull_direct(int op, const LaunchArgs& a, cudaStream_t s) {
                                  : dispatch_dp<kPull, long long, false>(a, grid, s);
         case kPullGrad: return small ? dispatch_dp<kPullGrad, int, false>(a, grid, s)
                                      : dispatch_dp<kPullGrad, long long, false>(a, grid, s);
-        default: return small ? dispatch_dp<kPullHess, int, false>(a, grid, s)
-                              : dispatch_dp<kPullHess, long long, false>(a, grid, s);
+        case kPullHess: return small ? dispatch_dp<kPullHess, int, false>(a, grid, s)
+                                     : dispatch_dp<kPullHess, long long, false>(a, grid, s);
+        case kPullGradDot: return small ? dispatch_dp<kPullGradDot, int, false>(a, grid, s)
+                                        : dispatch_dp<kPullGradDot, long long, false>(a, grid, s);
+        default: return small ? dispatch_dp<kPullHessDot, int, false>(a, grid, s)
+                              : dispatch_dp<kPullHessDot, long long, false>(a, grid, s);
     }
 }
 

@@ -70,6 +70,8 @@ struct Box {
     int P, Q, size; // row pitch (P % 32 == pmod, P % 4 == 0), plane pitch (multiple of 32), floats
     int mode;       // 0 no valid voxel, 1 shared memory, 2 per-voxel global fallback
     int interior;   // bit k: the box lies inside the image along dimension k (no folding)
+    float S;        // block sum of the caller's per-thread value (push: bound on sum |contribution|)
+    int E;          // scale exponent of the fixed-point accumulator for S (see scale_exponent)
 };
 
 __device__ __forceinline__ int clamp_tap(long long o) {
@@ -80,26 +82,46 @@ __device__ __forceinline__ int first_tap_i(float x, int DP) {
     return clamp_tap((long long)ceilf(__fsub_rn(x, 0.5f * (float)DP)));
 }
 
+// Exponent E of the fixed-point accumulator scale for a bound S on the sum of
+// |contributions|: S < 2^E.  INT_MAX: nothing to accumulate (S == 0);
+// INT_MIN: S non-finite or outside the range the scale factors cover, so the
+// tile accumulates in float instead.
+__device__ __forceinline__ int scale_exponent(float S) {
+    if (S == 0.f) return INT_MAX;
+    if (!(S > 0.f) || !finitef(S)) return INT_MIN;
+    int E;
+    frexpf(S * 1.0009765625f, &E);
+    return (E < -80 || E > 100) ? INT_MIN : E;
+}
+
 // Block-wide reduction of the first-tap bounds into the footprint box.
 // `words` = shared-memory words needed per box element (1 for pull, 2 for push).
+// Also sums `ssum` over the block into box.S (fixed order) and sets box.E.
 template <int DP>
 __device__ __forceinline__ void reduce_box(int (&mn)[3], int (&mx)[3], const TileGrid& t, const Geometry& g,
-                                           int words, Box& box, int (&red)[8][6]) {
+                                           int words, Box& box, int (&red)[8][7], float ssum = 0.f) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         mn[k] = __reduce_min_sync(0xffffffffu, mn[k]);
         mx[k] = __reduce_max_sync(0xffffffffu, mx[k]);
     }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) ssum += __shfl_xor_sync(0xffffffffu, ssum, off);
     if (lane == 0) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             red[warp][k] = mn[k];
             red[warp][3 + k] = mx[k];
         }
+        red[warp][6] = __float_as_int(ssum);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
+        float S = 0.f;
+        for (int w = 0; w < kThreads / 32; ++w) S += __int_as_float(red[w][6]);
+        box.S = S;
+        box.E = scale_exponent(S);
         int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
 #pragma unroll
         for (int w = 0; w < kThreads / 32; ++w)
@@ -431,12 +453,13 @@ struct Ring {
     unsigned bars;     // shared address of the first mbarrier
 };
 
-// Fill ring slot (j % kStages) with tile T: deformation components 0..2 and, for
-// push, NVAL value components of channel 0.  Called by every thread.
+// Fill ring slot (j % kStages) with tile T: deformation components 0..2 and
+// NVAL value components of channel 0 of `vals` (layout (d1, NVAL, nc, nb); the
+// push input, or the fused step's target).  Called by every thread.
 template <int V, int NVAL, bool TMA, typename IT>
 __device__ __forceinline__ void ring_fill(const Ring& r, int j, int T, const LaunchArgs& a, const TileGrid& t,
                                           const ThreadVox<V>& tv, const CUtensorMap& phimap,
-                                          const CUtensorMap& valmap) {
+                                          const CUtensorMap& valmap, const float* vals) {
     constexpr int NV = kThreads * V;
     float* slot = r.base + (j % kStages) * r.slot_floats;
     const TileOrigin o = tile_origin(t, T);
@@ -452,7 +475,7 @@ __device__ __forceinline__ void ring_fill(const Ring& r, int j, int T, const Lau
     } else {
         const long long n1 = a.g.n1;
         const float* phi = a.phi + (long long)o.b * 3 * n1;
-        const float* val = a.in + (long long)o.b * a.g.nc * NVAL * n1;
+        const float* val = vals + (long long)o.b * a.g.nc * NVAL * n1;
 #pragma unroll
         for (int q = 0; q < V; ++q) {
             const int lin = threadIdx.x + q * kThreads;
@@ -497,15 +520,18 @@ __device__ __forceinline__ void tile_bounds(const Geometry& g, const TileOrigin&
     }
 }
 
-// Evaluate channel c of a tile for the pull family.
-template <int DP, int OP, int V, typename IT>
+// Evaluate channel c of a tile for the pull family (dot ops accumulate into
+// acc[q] and store after the last channel).
+template <int DP, int OP_, int V, typename IT>
 __device__ __forceinline__ void pull_compute(const LaunchArgs& a, const TileOrigin& o, const ThreadVox<V>& tv,
-                                             const float* slot, int c, const Box& box, const float* sm) {
-    constexpr int NCOMP = pull_ncomp<OP>();
+                                             const float* slot, int c, const Box& box, const float* sm,
+                                             float (&acc)[V][3]) {
+    constexpr int OP = pull_base_op<OP_>();
+    constexpr int NCOMP = pull_ncomp<OP_>();
     constexpr int NV = kThreads * V;
     const Geometry& g = a.g;
     const long long n1 = g.n1;
-    float* outc = a.out + ((long long)o.b * g.nc + c) * NCOMP * n1;
+    const bool last = c == g.nc - 1;
 #pragma unroll
     for (int q = 0; q < V; ++q) {
         const IT v = tv.template index<IT>(o, q);
@@ -513,24 +539,38 @@ __device__ __forceinline__ void pull_compute(const LaunchArgs& a, const TileOrig
         const int lin = threadIdx.x + q * kThreads;
         float x0, x1, x2;
         if (!load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2)) {
+            if (!pull_is_dot<OP_>() || last) {
+                float* out = pull_out<OP_>(a, o.b, c, (long long)v);
 #pragma unroll
-            for (int p = 0; p < NCOMP; ++p) outc[(long long)p * n1 + v] = qnan();
+                for (int p = 0; p < NCOMP; ++p) out[(long long)p * n1] = qnan();
+            }
             continue;
         }
         if (box.mode != 1) {
-            if (c == 0) pull_tile_fallback<DP, OP, IT>(a, o.b, (long long)v, x0, x1, x2);
+            if (c == 0) pull_tile_fallback<DP, OP_, IT>(a, o.b, (long long)v, x0, x1, x2);
             continue;
         }
-        W3<DP, OP> wx, wy, wz;
-        const int ox = spline_taps32<DP, OP>(x0, wx.w, wx.dw, wx.hw) - box.xo;
-        const int oy = spline_taps32<DP, OP>(x1, wy.w, wy.dw, wy.hw) - box.lo[1];
-        const int oz = spline_taps32<DP, OP>(x2, wz.w, wz.dw, wz.hw) - box.lo[2];
+        constexpr int ORD = op_order(OP);
+        W3<DP, ORD> wx, wy, wz;
+        const int ox = spline_taps32<DP, ORD>(x0, wx.w, wx.dw, wx.hw) - box.xo;
+        const int oy = spline_taps32<DP, ORD>(x1, wy.w, wy.dw, wy.hw) - box.lo[1];
+        const int oz = spline_taps32<DP, ORD>(x2, wz.w, wz.dw, wz.hw) - box.lo[2];
         const unsigned P4 = 4u * box.P, Q4 = 4u * box.Q;
         const unsigned p = smem_addr(sm) + 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
         float r[6];
         contract<OP, DP>(wx, wy, wz, DP, DP, DP, false,
                          [&](int k, int j, int i) { return lds_f32(p + k * Q4 + j * P4 + 4u * i); }, r);
-        pull_store<OP>(outc + v, n1, r);
+        if constexpr (pull_is_dot<OP_>()) {
+            dot_accumulate<OP_>(a, o.b, c, (long long)v, r, acc[q]);
+            if (last) {
+                float* out = pull_out<OP_>(a, o.b, 0, (long long)v);
+                out[0] = acc[q][0];
+                out[n1] = acc[q][1];
+                out[2 * n1] = acc[q][2];
+            }
+        } else {
+            pull_store<OP>(pull_out<OP_>(a, o.b, c, (long long)v), n1, r);
+        }
     }
 }
 
@@ -544,7 +584,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pull_tiled(const __grid_constan
                                                             const __grid_constant__ CUtensorMap phimap) {
     extern __shared__ __align__(128) float4 smem4[];
     constexpr int NV = kThreads * V;
-    __shared__ int red[8][6];
+    __shared__ int red[8][7];
     __shared__ Box boxm[2];
     __shared__ int s_abort;
     const Geometry& g = a.g;
@@ -569,7 +609,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pull_tiled(const __grid_constan
     }
     __syncthreads();
     for (int j = 0; j < kStages && j < ntl; ++j)
-        ring_fill<V, 0, TMA, IT>(ring, j, T0 + j * G, a, t, tv, phimap, phimap);
+        ring_fill<V, 0, TMA, IT>(ring, j, T0 + j * G, a, t, tv, phimap, phimap, a.in);
     if (!TMA) __syncthreads();
 
     // box of tile j (its deformation must be in the ring), staged into buffer j & 1
@@ -602,7 +642,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_pull_tiled(const __grid_constan
         const float* slot = ring.base + (j % kStages) * ring.slot_floats;
         const Box& box = boxm[j & 1];
         float* buf = bufs + (j & 1) * t.cap;
-        pull_compute<DP, OP, V, IT>(a, o, tv, slot, 0, box, buf);
+        float acc[V][3];
+#pragma unroll
+        for (int q = 0; q < V; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.f;
+        pull_compute<DP, OP, V, IT>(a, o, tv, slot, 0, box, buf, acc);
         for (int c = 1; c < g.nc; ++c) {
             __syncthreads();   // channel c-1 reads of the buffer are done
             if (box.mode == 1) {
@@ -612,21 +655,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_pull_tiled(const __grid_constan
                 asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
             }
             __syncthreads();
-            pull_compute<DP, OP, V, IT>(a, o, tv, slot, c, box, buf);
+            pull_compute<DP, OP, V, IT>(a, o, tv, slot, c, box, buf, acc);
         }
         __syncthreads();   // ring slot j and buffer j & 1 are free
         if (j + kStages < ntl)
-            ring_fill<V, 0, TMA, IT>(ring, j + kStages, T0 + (j + kStages) * G, a, t, tv, phimap, phimap);
+            ring_fill<V, 0, TMA, IT>(ring, j + kStages, T0 + (j + kStages) * G, a, t, tv, phimap, phimap, a.in);
         if (!TMA) __syncthreads();
     }
 }
 
 // Scatter one voxel into the push accumulator (box-relative first taps ox, oy, oz).
 // FIXED: two int32 words per element (values pre-scaled to q1 units); otherwise float.
-template <int DP, int OP, bool FIXED>
-__device__ __forceinline__ void push_scatter(const W3<DP, OP == kPushGrad ? 1 : 0>& wx,
-                                             const W3<DP, OP == kPushGrad ? 1 : 0>& wy,
-                                             const W3<DP, OP == kPushGrad ? 1 : 0>& wz, float v0, float v1, float v2,
+// WT: any weight set with w (and dw for push_grad) of DP taps.
+template <int DP, int OP, bool FIXED, class WT>
+__device__ __forceinline__ void push_scatter(const WT& wx, const WT& wy, const WT& wz, float v0, float v1, float v2,
                                              unsigned base, unsigned P4, unsigned Q4, unsigned lo_off) {
 #pragma unroll
     for (int k = 0; k < DP; ++k) {
@@ -664,7 +706,8 @@ __device__ __forceinline__ void push_scatter(const W3<DP, OP == kPushGrad ? 1 : 
 
 // Persistent push family.  The ring holds each tile's deformation and its
 // channel-0 values kStages tiles ahead; the tile scatters into the shared
-// accumulator and flushes it with global reductions.
+// accumulator and flushes it with global reductions.  The flush clears every
+// element it reads, so the accumulator is zero again for the next tile.
 template <int DP, int OP, int V, typename IT, bool TMA>
 __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constant__ LaunchArgs a,
                                                             const __grid_constant__ TileGrid t,
@@ -674,10 +717,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
     constexpr int ORD = OP == kPushGrad ? 1 : 0;
     constexpr int NCOMP = OP == kPushGrad ? 3 : 1;
     constexpr int NV = kThreads * V;
-    __shared__ int red[8][6];
+    __shared__ int red[8][7];
     __shared__ float sred[8];
     __shared__ Box box;
-    __shared__ int s_exp;
     __shared__ int s_abort;
     const Geometry& g = a.g;
     const long long n1 = g.n1;
@@ -694,6 +736,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
     ring.slot_floats = (3 + NCOMP) * NV;
     float* accf = sm + kStages * (3 + NCOMP) * NV;
     ring.bars = smem_addr(accf + t.cap);
+    for (int i = threadIdx.x; i < (t.cap >> 2); i += kThreads)
+        reinterpret_cast<float4*>(accf)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (threadIdx.x == 0) {
         s_abort = 0;
         if (TMA) {
@@ -703,7 +747,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
     }
     __syncthreads();
     for (int j = 0; j < kStages && j < ntl; ++j)
-        ring_fill<V, NCOMP, TMA, IT>(ring, j, T0 + j * G, a, t, tv, phimap, valmap);
+        ring_fill<V, NCOMP, TMA, IT>(ring, j, T0 + j * G, a, t, tv, phimap, valmap, a.in);
     if (!TMA) __syncthreads();
 
     const unsigned acc_base = smem_addr(accf);
@@ -711,9 +755,28 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
         const TileOrigin o = tile_origin(t, T0 + j * G);
         const float* slot = ring.base + (j % kStages) * ring.slot_floats;
         if (!ring_wait<TMA>(ring, j)) s_abort = 1;
+        // deformation validity, first-tap bounds and the channel-0 scale bound
         int mn[3], mx[3];
         tile_bounds<DP, V, IT>(g, o, tv, slot, mn, mx);
-        reduce_box<DP>(mn, mx, t, g, 2, box, red);
+        float bound0 = 0.f;
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+            const int lin = threadIdx.x + q * kThreads;
+            float x0, x1, x2;
+            if (tv.template index<IT>(o, q) < 0 ||
+                !load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2))
+                continue;
+            bool fin = true;
+            float s1 = 0.f;
+#pragma unroll
+            for (int p = 0; p < NCOMP; ++p) {
+                const float v = slot[(3 + p) * NV + lin];
+                fin = fin && finitef(v);
+                s1 += fabsf(v);
+            }
+            if (fin) bound0 += OP == kPushGrad ? 2.f * s1 : s1;
+        }
+        reduce_box<DP>(mn, mx, t, g, 2, box, red, bound0);
         if (s_abort) break;
         if (box.mode == 2) {
 #pragma unroll
@@ -726,68 +789,60 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
             }
         } else if (box.mode == 1) {
             const unsigned lo_off = 4u * (unsigned)box.size;
-            const int* acc_hi = reinterpret_cast<const int*>(accf);
-            const int* acc_lo = acc_hi + box.size;
+            int* acc_hi = reinterpret_cast<int*>(accf);
+            int* acc_lo = acc_hi + box.size;
             const float* inb = a.in + (long long)o.b * g.nc * NCOMP * n1;
             for (int c = 0; c < g.nc; ++c) {
                 int b0, b1, b2;
                 bnd_code(a, c, b0, b1, b2);
-                float val[V][NCOMP];
-                float bound = 0.f;
-                unsigned live = 0;
+                int E = box.E;
+                if (c > 0) {
+                    // values of channel c straight from global memory, and their scale bound
+                    float bound = 0.f;
 #pragma unroll
-                for (int q = 0; q < V; ++q) {
-                    const IT v = tv.template index<IT>(o, q);
-                    const int lin = threadIdx.x + q * kThreads;
+                    for (int q = 0; q < V; ++q) {
+                        const IT v = tv.template index<IT>(o, q);
+                        const int lin = threadIdx.x + q * kThreads;
+                        float x0, x1, x2;
+                        if (v < 0 || !load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2))
+                            continue;
+                        bool fin = true;
+                        float s1 = 0.f;
 #pragma unroll
-                    for (int p = 0; p < NCOMP; ++p)
-                        val[q][p] = c == 0 ? slot[(3 + p) * NV + lin]
-                                           : (v < 0 ? 0.f : __ldg(inb + (long long)c * NCOMP * n1 + v + p * n1));
-                    float x0, x1, x2;
-                    if (v < 0 || !load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2)) continue;
-                    bool fin = true;
-                    float s1 = 0.f;
-#pragma unroll
-                    for (int p = 0; p < NCOMP; ++p) {
-                        fin = fin && finitef(val[q][p]);
-                        s1 += fabsf(val[q][p]);
+                        for (int p = 0; p < NCOMP; ++p) {
+                            const float vv = __ldg(inb + (long long)c * NCOMP * n1 + v + p * n1);
+                            fin = fin && finitef(vv);
+                            s1 += fabsf(vv);
+                        }
+                        if (fin) bound += OP == kPushGrad ? 2.f * s1 : s1;
                     }
-                    if (!fin) continue;
-                    bound += OP == kPushGrad ? 2.f * s1 : s1;
-                    live |= 1u << q;
-                }
 #pragma unroll
-                for (int off = 16; off > 0; off >>= 1) bound += __shfl_xor_sync(0xffffffffu, bound, off);
-                if (c > 0) __syncthreads();   // previous channel's flush is done with the box and sred
-                if (lane == 0) sred[warp] = bound;
-                __syncthreads();
-                if (threadIdx.x == 0) {
+                    for (int off = 16; off > 0; off >>= 1) bound += __shfl_xor_sync(0xffffffffu, bound, off);
+                    __syncthreads();   // the previous channel's flush is done
+                    if (lane == 0) sred[warp] = bound;
+                    __syncthreads();
                     float S = 0.f;
                     for (int w = 0; w < kThreads / 32; ++w) S += sred[w];
-                    int E = 0;
-                    // fixed point needs 0 < S < inf and 2^(43-E), 2^(E-43) representable
-                    if (S > 0.f && finitef(S)) {
-                        frexpf(S * 1.0009765625f, &E);
-                        if (E < -80 || E > 100) E = INT_MIN;
-                    } else {
-                        E = S == 0.f ? INT_MAX : INT_MIN;   // INT_MAX: nothing to add
-                    }
-                    s_exp = E;
+                    E = scale_exponent(S);
                 }
-                for (int i = threadIdx.x; i < (2 * box.size) >> 2; i += kThreads)
-                    reinterpret_cast<float4*>(accf)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-                __syncthreads();
-                const int E = s_exp;
                 if (E == INT_MAX) continue;   // every value of this channel is zero or skipped
                 const bool fixed = E != INT_MIN;
                 FixedScale fs;
                 fs.set(fixed ? E : 0);
 #pragma unroll
                 for (int q = 0; q < V; ++q) {
-                    if (!(live >> q & 1)) continue;
+                    const IT v = tv.template index<IT>(o, q);
                     const int lin = threadIdx.x + q * kThreads;
                     float x0, x1, x2;
-                    load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2);
+                    if (v < 0 || !load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2)) continue;
+                    float val[NCOMP];
+                    bool fin = true;
+#pragma unroll
+                    for (int p = 0; p < NCOMP; ++p) {
+                        val[p] = c == 0 ? slot[(3 + p) * NV + lin] : __ldg(inb + (long long)c * NCOMP * n1 + v + p * n1);
+                        fin = fin && finitef(val[p]);
+                    }
+                    if (!fin) continue;
                     W3<DP, ORD> wx, wy, wz;
                     const int ox = spline_taps32<DP, ORD>(x0, wx.w, wx.dw, wx.hw) - box.xo;
                     const int oy = spline_taps32<DP, ORD>(x1, wy.w, wy.dw, wy.hw) - box.lo[1];
@@ -795,24 +850,465 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
                     const unsigned P4 = 4u * box.P, Q4 = 4u * box.Q;
                     const unsigned base = acc_base + 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
                     const float sc = fixed ? fs.inv_q1 : 1.f;
-                    const float w0 = val[q][0] * sc, w1 = NCOMP > 1 ? val[q][NCOMP > 1 ? 1 : 0] * sc : 0.f,
-                                w2 = NCOMP > 2 ? val[q][NCOMP > 2 ? 2 : 0] * sc : 0.f;
+                    const float w0 = val[0] * sc;
+                    const float w1 = NCOMP > 1 ? val[NCOMP > 1 ? 1 : 0] * sc : 0.f;
+                    const float w2 = NCOMP > 2 ? val[NCOMP > 2 ? 2 : 0] * sc : 0.f;
                     if (fixed) push_scatter<DP, OP, true>(wx, wy, wz, w0, w1, w2, base, P4, Q4, lo_off);
                     else push_scatter<DP, OP, false>(wx, wy, wz, w0, w1, w2, base, P4, Q4, lo_off);
                 }
-                __syncthreads();
+                __syncthreads();   // the scatter is complete
                 float* f0 = a.out + ((long long)o.b * g.nc + c) * g.n0;
                 if (fixed)
-                    flush_box<IT>(box, g, b0, b1, b2, f0,
-                                  [&](int si) { return fixed_value(acc_hi[si], acc_lo[si], fs); });
+                    flush_box<IT>(box, g, b0, b1, b2, f0, [&](int si) {
+                        const float v = fixed_value(acc_hi[si], acc_lo[si], fs);
+                        acc_hi[si] = 0;
+                        acc_lo[si] = 0;
+                        return v;
+                    });
                 else
-                    flush_box<IT>(box, g, b0, b1, b2, f0, [&](int si) { return accf[si]; });
+                    flush_box<IT>(box, g, b0, b1, b2, f0, [&](int si) {
+                        const float v = accf[si];
+                        accf[si] = 0.f;
+                        return v;
+                    });
             }
         }
-        __syncthreads();   // ring slot j and the accumulator are free
+        __syncthreads();   // ring slot j is free and the accumulator is clear
         if (j + kStages < ntl)
-            ring_fill<V, NCOMP, TMA, IT>(ring, j + kStages, T0 + (j + kStages) * G, a, t, tv, phimap, valmap);
+            ring_fill<V, NCOMP, TMA, IT>(ring, j + kStages, T0 + (j + kStages) * G, a, t, tv, phimap, valmap, a.in);
         if (!TMA) __syncthreads();
+    }
+}
+
+// ---- fused forward + adjoint step ------------------------------------------
+//
+// loss = sum_{b,c,v} (pull(f_c, phi)[v] - g_c[v])^2, df = push(2 r), and
+// dphi[v] = sum_c 2 r_c grad pull(f_c)[v]: the forward pull, the pull rrule's
+// two cotangents (src/pushpull_pb.jl:11-18) and the loss of the differentiable
+// step in one pass.  The image box is staged once per (tile, channel) and serves
+// both the value and the gradient; delta = 2 r is scattered into the shared
+// accumulator of the same box and flushed with global reductions.
+
+// Per-voxel global-memory version of one channel (tiles whose box does not fit):
+// returns the residual r and the gradient; scatters 2 r into df with atomics.
+template <int DP, typename IT>
+__device__ __noinline__ float fused_voxel_global(const LaunchArgs& a, int b, int c, long long v, float x0, float x1,
+                                                 float x2, float gv, float (&grad)[3]) {
+    const Geometry& g = a.g;
+    const IT sy = (IT)g.d0[0];
+    const IT sz = (IT)(g.d0[0] * g.d0[1]);
+    int b0, b1, b2;
+    bnd_code(a, c, b0, b1, b2);
+    Axis<DP, 1, IT> ax, ay, az;
+    ax.setup(x0, g.dp[0], b0, g.d0[0], (IT)1);
+    ay.setup(x1, g.dp[1], b1, g.d0[1], sy);
+    az.setup(x2, g.dp[2], b2, g.d0[2], sz);
+    const float* f0 = a.in + ((long long)b * g.nc + c) * g.n0;
+    float r[6];
+    contract<kPullValGrad, DP>(ax, ay, az, DP, DP, DP, false,
+                               [&](int k, int j, int i) { return __ldg(f0 + (az.off[k] + ay.off[j] + ax.off[i])); }, r);
+    grad[0] = r[0];
+    grad[1] = r[1];
+    grad[2] = r[2];
+    const float res = r[3] - gv;
+    const float d = 2.f * res;
+    if (finitef(d)) {
+        float* df = a.out + ((long long)b * g.nc + c) * g.n0;
+#pragma unroll
+        for (int k = 0; k < DP; ++k)
+#pragma unroll
+            for (int j = 0; j < DP; ++j) {
+                const float cb = d * (ay.w[j] * az.w[k]);
+#pragma unroll
+                for (int i = 0; i < DP; ++i) atomicAdd(df + (az.off[k] + ay.off[j] + ax.off[i]), cb * ax.w[i]);
+            }
+    }
+    return res;
+}
+
+template <int DP, int V, typename IT, bool TMA>
+__global__ void __launch_bounds__(kThreads, 2) k_fused_tiled(const __grid_constant__ LaunchArgs a,
+                                                             const __grid_constant__ TileGrid t,
+                                                             const __grid_constant__ CUtensorMap phimap,
+                                                             const __grid_constant__ CUtensorMap gmap) {
+    extern __shared__ __align__(128) float4 smem4[];
+    constexpr int NV = kThreads * V;
+    __shared__ int red[8][7];
+    __shared__ float sred[8];
+    __shared__ double dred[8];
+    __shared__ Box boxm[2];
+    __shared__ int s_abort;
+    const Geometry& g = a.g;
+    const long long n1 = g.n1;
+    const int G = gridDim.x;
+    const int T0 = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ntl = T0 < t.ntiles ? (t.ntiles - T0 + G - 1) / G : 0;
+    const ThreadVox<V> tv(t, g);
+    double loss = 0.0;
+
+    float* sm = reinterpret_cast<float*>(smem4);
+    Ring ring;
+    ring.base = sm;
+    ring.slot_floats = 4 * NV;                       // deformation + channel-0 target
+    float* bufs = sm + kStages * 4 * NV;              // image box, double buffered
+    float* accf = bufs + 2 * t.cap;                   // adjoint accumulator: 2 words per element
+    ring.bars = smem_addr(accf + 2 * t.cap);
+    for (int i = threadIdx.x; i < (2 * t.cap) >> 2; i += kThreads)
+        reinterpret_cast<float4*>(accf)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (threadIdx.x == 0) {
+        s_abort = 0;
+        if (TMA) {
+            for (int k = 0; k < kStages; ++k) mbar_init(ring.bars + 8u * k, 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+    }
+    __syncthreads();
+    for (int j = 0; j < kStages && j < ntl; ++j)
+        ring_fill<V, 1, TMA, IT>(ring, j, T0 + j * G, a, t, tv, phimap, gmap, a.up);
+    if (!TMA) __syncthreads();
+
+    // Box of tile j and the channel-0 scale bound: |r| <= max|f| + |g| because the
+    // B-spline weights are non-negative and sum to one, so the sum of |2 r w|
+    // over a voxel's taps is at most 2 (max|f| + |g|).
+    auto prepare = [&](int j) {
+        const TileOrigin o = tile_origin(t, T0 + j * G);
+        const float* slot = ring.base + (j % kStages) * ring.slot_floats;
+        if (!ring_wait<TMA>(ring, j)) s_abort = 1;
+        int mn[3], mx[3];
+        tile_bounds<DP, V, IT>(g, o, tv, slot, mn, mx);
+        const float M = __uint_as_float(a.fmax[(long long)o.b * g.nc]);
+        float bound = 0.f;
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+            const int lin = threadIdx.x + q * kThreads;
+            float x0, x1, x2;
+            if (tv.template index<IT>(o, q) >= 0 &&
+                load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2))
+                bound += 2.f * (M + fabsf(slot[3 * NV + lin]));
+        }
+        reduce_box<DP>(mn, mx, t, g, 1, boxm[j & 1], red, bound);
+        if (boxm[j & 1].mode == 1) {
+            int b0, b1, b2;
+            bnd_code(a, 0, b0, b1, b2);
+            stage_box<IT>(boxm[j & 1], g, b0, b1, b2, a.in + (long long)o.b * g.nc * g.n0, bufs + (j & 1) * t.cap);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+
+    if (ntl > 0) prepare(0);
+    const unsigned acc_base = smem_addr(accf);
+    int* acc_hi = reinterpret_cast<int*>(accf);
+    for (int j = 0; j < ntl; ++j) {
+        if (j + 1 < ntl) {
+            prepare(j + 1);
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        }
+        __syncthreads();   // box j is in its buffer
+        if (s_abort) break;
+        const TileOrigin o = tile_origin(t, T0 + j * G);
+        const float* slot = ring.base + (j % kStages) * ring.slot_floats;
+        const Box& box = boxm[j & 1];
+        float* buf = bufs + (j & 1) * t.cap;
+        const unsigned lo_off = 4u * (unsigned)box.size;
+        int* acc_lo = acc_hi + box.size;
+        float dphi[V][3];
+        unsigned valid = 0;
+#pragma unroll
+        for (int q = 0; q < V; ++q) dphi[q][0] = dphi[q][1] = dphi[q][2] = 0.f;
+        for (int c = 0; c < g.nc; ++c) {
+            int b0, b1, b2;
+            bnd_code(a, c, b0, b1, b2);
+            const float* gc = a.up + ((long long)o.b * g.nc + c) * n1;
+            int E = box.E;
+            if (c > 0) {
+                __syncthreads();   // channel c-1 is done with the box and the accumulator
+                if (box.mode == 1) {
+                    stage_box<IT>(box, g, b0, b1, b2, a.in + ((long long)o.b * g.nc + c) * g.n0, buf);
+                    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+                }
+                const float M = __uint_as_float(a.fmax[(long long)o.b * g.nc + c]);
+                float bound = 0.f;
+#pragma unroll
+                for (int q = 0; q < V; ++q) {
+                    const IT v = tv.template index<IT>(o, q);
+                    if (v >= 0 && (valid >> q & 1)) bound += 2.f * (M + fabsf(__ldg(gc + v)));
+                }
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) bound += __shfl_xor_sync(0xffffffffu, bound, off);
+                if (lane == 0) sred[warp] = bound;
+                __syncthreads();   // the box of channel c and every warp's bound are in
+                float S = 0.f;
+                for (int w = 0; w < kThreads / 32; ++w) S += sred[w];
+                E = scale_exponent(S);
+            }
+            const bool fixed = E != INT_MIN && E != INT_MAX;
+            FixedScale fs;
+            fs.set(fixed ? E : 0);
+#pragma unroll
+            for (int q = 0; q < V; ++q) {
+                const IT v = tv.template index<IT>(o, q);
+                if (v < 0) continue;
+                const int lin = threadIdx.x + q * kThreads;
+                float x0, x1, x2;
+                if (!load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2)) {
+                    loss += (double)qnan();   // pull is NaN here, and so is the loss
+                    continue;
+                }
+                valid |= 1u << q;
+                const float gv = c == 0 ? slot[3 * NV + lin] : __ldg(gc + v);
+                float res, grad[3];
+                if (box.mode == 1) {
+                    W3<DP, 1> wx, wy, wz;
+                    const int ox = spline_taps32<DP, 1>(x0, wx.w, wx.dw, wx.hw) - box.xo;
+                    const int oy = spline_taps32<DP, 1>(x1, wy.w, wy.dw, wy.hw) - box.lo[1];
+                    const int oz = spline_taps32<DP, 1>(x2, wz.w, wz.dw, wz.hw) - box.lo[2];
+                    const unsigned P4 = 4u * box.P, Q4 = 4u * box.Q;
+                    const unsigned off = 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
+                    const unsigned p = smem_addr(buf) + off;
+                    float r[6];
+                    contract<kPullValGrad, DP>(wx, wy, wz, DP, DP, DP, false,
+                                               [&](int k, int jj, int i) { return lds_f32(p + k * Q4 + jj * P4 + 4u * i); },
+                                               r);
+                    res = r[3] - gv;
+                    grad[0] = r[0];
+                    grad[1] = r[1];
+                    grad[2] = r[2];
+                    const float d = 2.f * res;
+                    if (finitef(d) && E != INT_MAX) {
+                        if (fixed)
+                            push_scatter<DP, kPush, true>(wx, wy, wz, d * fs.inv_q1, 0.f, 0.f, acc_base + off, P4, Q4,
+                                                          lo_off);
+                        else
+                            push_scatter<DP, kPush, false>(wx, wy, wz, d, 0.f, 0.f, acc_base + off, P4, Q4, lo_off);
+                    }
+                } else {
+                    res = fused_voxel_global<DP, IT>(a, o.b, c, (long long)v, x0, x1, x2, gv, grad);
+                }
+                loss += (double)(res * res);
+                const float d = 2.f * res;
+                dphi[q][0] = fmaf(d, grad[0], dphi[q][0]);
+                dphi[q][1] = fmaf(d, grad[1], dphi[q][1]);
+                dphi[q][2] = fmaf(d, grad[2], dphi[q][2]);
+            }
+            __syncthreads();   // the scatter is complete
+            if (box.mode == 1 && E != INT_MAX) {
+                float* df = a.out + ((long long)o.b * g.nc + c) * g.n0;
+                if (fixed)
+                    flush_box<IT>(box, g, b0, b1, b2, df, [&](int si) {
+                        const float v = fixed_value(acc_hi[si], acc_lo[si], fs);
+                        acc_hi[si] = 0;
+                        acc_lo[si] = 0;
+                        return v;
+                    });
+                else
+                    flush_box<IT>(box, g, b0, b1, b2, df, [&](int si) {
+                        const float v = accf[si];
+                        accf[si] = 0.f;
+                        return v;
+                    });
+            }
+        }
+        // deformation cotangent of every sample voxel of the tile
+        float* dp = a.out2 + (long long)o.b * 3 * n1;
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+            const IT v = tv.template index<IT>(o, q);
+            if (v < 0) continue;
+            const bool ok = valid >> q & 1;
+            dp[v] = ok ? dphi[q][0] : qnan();
+            dp[v + n1] = ok ? dphi[q][1] : qnan();
+            dp[v + 2 * n1] = ok ? dphi[q][2] : qnan();
+        }
+        __syncthreads();   // ring slot j, the box buffer and the accumulator are free
+        if (j + kStages < ntl)
+            ring_fill<V, 1, TMA, IT>(ring, j + kStages, T0 + (j + kStages) * G, a, t, tv, phimap, gmap, a.up);
+        if (!TMA) __syncthreads();
+    }
+    // this CTA's loss partial
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
+    if (lane == 0) dred[warp] = loss;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) sum += dred[w];
+        a.partial[blockIdx.x] = sum;
+    }
+}
+
+
+// ---- batched uneven workload ------------------------------------------------
+//
+// Tiles of all items form one queue; a CTA takes the next tile with an atomic
+// counter (dynamic load balance over volumes of uneven size and degree),
+// evaluates pull for the tile from its staged image box, writes f1, and pushes
+// the same values through the same box into the shared accumulator, which it
+// flushes into the item's output.  Shared memory is split into a fixed
+// accumulator region (two words per element) and the image box.
+
+template <int DP>
+__device__ __forceinline__ void batch_tile(const BatchItem& it, int lt, float* sm, int cap, Box& box,
+                                           int (&red)[8][7], float (&sred)[8]) {
+    constexpr int V = 2;
+    constexpr int NV = kThreads * V;
+    const LaunchArgs& a = it.pull;
+    const LaunchArgs& pb = it.push;
+    const Geometry& g = a.g;
+    const long long n1 = g.n1;
+    const TileGrid& t = it.t;
+    const ThreadVox<V> tv(t, g);
+    const TileOrigin o = tile_origin(t, lt);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int accw = ((2 * cap / 3) + 3) & ~3;   // accumulator words (fixed region)
+    float* accf = sm;
+    float* fbox = sm + accw;
+
+    float X[V][3];
+    int iv[V];
+    unsigned ok = 0;
+    int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+        iv[q] = tv.template index<int>(o, q);
+        if (iv[q] < 0) continue;
+        const float* phi = a.phi + iv[q];
+        if (!load_valid(__ldg(phi), __ldg(phi + n1), __ldg(phi + 2 * n1), g, X[q][0], X[q][1], X[q][2])) continue;
+        ok |= 1u << q;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int f = first_tap32(X[q][k], DP);
+            const int cl = f < -kClamp ? -kClamp : (f > kClamp ? kClamp : f);
+            mn[k] = min(mn[k], cl);
+            mx[k] = max(mx[k], cl);
+        }
+    }
+    reduce_box<DP>(mn, mx, t, g, 3, box, red);   // 3 words per element: 2 accumulator + 1 image
+    if (box.mode != 1) {
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+            if (iv[q] < 0) continue;
+            if (!(ok >> q & 1)) {
+                pull_voxel_nan<kPull>(a, 0, iv[q]);
+                continue;
+            }
+            pull_tile_fallback<DP, kPull, int>(a, 0, iv[q], X[q][0], X[q][1], X[q][2]);
+            push_tile_fallback<DP, kPush, int>(pb, 0, iv[q], X[q][0], X[q][1], X[q][2]);
+        }
+        __syncthreads();   // box record reused by the next tile
+        return;
+    }
+    const unsigned acc_base = smem_addr(accf);
+    const unsigned lo_off = 4u * (unsigned)box.size;
+    int* acc_hi = reinterpret_cast<int*>(accf);
+    int* acc_lo = acc_hi + box.size;
+    for (int c = 0; c < g.nc; ++c) {
+        int b0, b1, b2;
+        bnd_code(a, c, b0, b1, b2);
+        stage_box<int>(box, g, b0, b1, b2, a.in + (long long)c * g.n0, fbox);
+        asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+        __syncthreads();
+        float val[V];
+        float bound = 0.f;
+        float* f1 = a.out + (long long)c * n1;
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+            val[q] = 0.f;
+            if (iv[q] < 0) continue;
+            if (!(ok >> q & 1)) {
+                f1[iv[q]] = qnan();
+                continue;
+            }
+            W3<DP, 0> wx, wy, wz;
+            const int ox = spline_taps32<DP, 0>(X[q][0], wx.w, wx.dw, wx.hw) - box.xo;
+            const int oy = spline_taps32<DP, 0>(X[q][1], wy.w, wy.dw, wy.hw) - box.lo[1];
+            const int oz = spline_taps32<DP, 0>(X[q][2], wz.w, wz.dw, wz.hw) - box.lo[2];
+            const unsigned P4 = 4u * box.P, Q4 = 4u * box.Q;
+            const unsigned p = smem_addr(fbox) + 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
+            float r[6];
+            contract<kPull, DP>(wx, wy, wz, DP, DP, DP, false,
+                                [&](int k, int jj, int i) { return lds_f32(p + k * Q4 + jj * P4 + 4u * i); }, r);
+            f1[iv[q]] = r[0];
+            val[q] = r[0];
+            if (finitef(r[0])) bound += fabsf(r[0]);
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) bound += __shfl_xor_sync(0xffffffffu, bound, off);
+        if (lane == 0) sred[warp] = bound;
+        __syncthreads();   // bounds in; the image box is no longer read
+        float S = 0.f;
+        for (int w = 0; w < kThreads / 32; ++w) S += sred[w];
+        const int E = scale_exponent(S);
+        if (E != INT_MAX) {
+            const bool fixed = E != INT_MIN;
+            FixedScale fs;
+            fs.set(fixed ? E : 0);
+#pragma unroll
+            for (int q = 0; q < V; ++q) {
+                if (!(ok >> q & 1) || !finitef(val[q])) continue;
+                W3<DP, 0> wx, wy, wz;
+                const int ox = spline_taps32<DP, 0>(X[q][0], wx.w, wx.dw, wx.hw) - box.xo;
+                const int oy = spline_taps32<DP, 0>(X[q][1], wy.w, wy.dw, wy.hw) - box.lo[1];
+                const int oz = spline_taps32<DP, 0>(X[q][2], wz.w, wz.dw, wz.hw) - box.lo[2];
+                const unsigned P4 = 4u * box.P, Q4 = 4u * box.Q;
+                const unsigned base = acc_base + 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
+                if (fixed) push_scatter<DP, kPush, true>(wx, wy, wz, val[q] * fs.inv_q1, 0.f, 0.f, base, P4, Q4, lo_off);
+                else push_scatter<DP, kPush, false>(wx, wy, wz, val[q], 0.f, 0.f, base, P4, Q4, lo_off);
+            }
+            __syncthreads();   // the scatter is complete
+            float* out = pb.out + (long long)c * g.n0;
+            if (fixed)
+                flush_box<int>(box, g, b0, b1, b2, out, [&](int si) {
+                    const float v = fixed_value(acc_hi[si], acc_lo[si], fs);
+                    acc_hi[si] = 0;
+                    acc_lo[si] = 0;
+                    return v;
+                });
+            else
+                flush_box<int>(box, g, b0, b1, b2, out, [&](int si) {
+                    const float v = accf[si];
+                    accf[si] = 0.f;
+                    return v;
+                });
+        }
+        __syncthreads();   // accumulator clear, image box and sred reusable
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchItem* __restrict__ items, int nitems, int total,
+                                                       unsigned* counter, int cap) {
+    extern __shared__ __align__(128) float4 smem4[];
+    __shared__ int red[8][7];
+    __shared__ float sred[8];
+    __shared__ Box box;
+    __shared__ int s_tile;
+    float* sm = reinterpret_cast<float*>(smem4);
+    const int accw = ((2 * cap / 3) + 3) & ~3;
+    for (int i = threadIdx.x; i < (accw >> 2); i += kThreads)
+        reinterpret_cast<float4*>(sm)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int T = s_tile;
+        __syncthreads();   // every thread has read the tile before the next claim
+        if (T >= total) break;
+        int lo = 0, hi = nitems - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (items[mid].tile_begin <= T) lo = mid;
+            else hi = mid - 1;
+        }
+        const BatchItem& it = items[lo];
+        const int lt = T - it.tile_begin;
+        switch (it.dp) {
+            case 1: batch_tile<1>(it, lt, sm, cap, box, red, sred); break;
+            case 2: batch_tile<2>(it, lt, sm, cap, box, red, sred); break;
+            case 3: batch_tile<3>(it, lt, sm, cap, box, red, sred); break;
+            case 4: batch_tile<4>(it, lt, sm, cap, box, red, sred); break;
+            default: batch_tile<5>(it, lt, sm, cap, box, red, sred); break;
+        }
     }
 }
 
@@ -934,6 +1430,36 @@ cudaError_t launch_v(const LaunchArgs& a, const TileGrid& t, cudaStream_t s) {
     }
 }
 
+template <int DP, int V, typename IT>
+cudaError_t launch_fused_v(const LaunchArgs& a, const TileGrid& t, cudaStream_t s, int grid) {
+    constexpr int NV = kThreads * V;
+    CUtensorMap phimap, gmap;
+    std::memset(&phimap, 0, sizeof phimap);
+    std::memset(&gmap, 0, sizeof gmap);
+    const long long nb = a.g.nb, nc = a.g.nc;
+    const bool tma = encode_tile_map(&phimap, a.phi, a.g.d1, 3 * nb, t, 3) &&
+                     encode_tile_map(&gmap, a.up, a.g.d1, nc * nb, t, 1);
+    const size_t smem = (size_t)kStages * 4 * NV * 4 + 4 * (size_t)t.cap * 4 + 8 * kStages;
+    cudaError_t e;
+    if (tma) {
+        auto k = k_fused_tiled<DP, V, IT, true>;
+        if ((e = opt_in(k, smem)) != cudaSuccess) return e;
+        k<<<grid, kThreads, smem, s>>>(a, t, phimap, gmap);
+    } else {
+        auto k = k_fused_tiled<DP, V, IT, false>;
+        if ((e = opt_in(k, smem)) != cudaSuccess) return e;
+        k<<<grid, kThreads, smem, s>>>(a, t, phimap, gmap);
+    }
+    return cudaGetLastError();
+}
+
+template <int DP, typename IT>
+cudaError_t launch_fused_dp(const LaunchArgs& a, const TileCfg& c, cudaStream_t s, int grid) {
+    const TileGrid t = make_grid(a, c);
+    if ((1 << (c.lx + c.ly + c.lz)) > kThreads) return launch_fused_v<DP, 2, IT>(a, t, s, grid);
+    return launch_fused_v<DP, 1, IT>(a, t, s, grid);
+}
+
 template <int DP, int OP, typename IT, bool PUSH>
 cudaError_t launch_one(const LaunchArgs& a, const TileCfg& c, cudaStream_t s) {
     const TileGrid t = make_grid(a, c);
@@ -961,6 +1487,12 @@ bool tiled_supported(const LaunchArgs& a, const TileCfg& t) {
     if (!(g.dp[0] == g.dp[1] && g.dp[1] == g.dp[2])) return false;
     // whole tiles of 256 or 512 voxels: every thread owns one voxel slot per V
     if (!(vox == kThreads || vox == 2 * kThreads) || t.cap < 64 || (t.cap & 3) || t.cap > 24 * 1024) return false;
+    // a tile must be mostly inside the sample grid: degenerate grids (e.g. a
+    // flat list of n1 samples) are better served by the per-voxel kernels
+    for (int k = 0; k < 3; ++k) {
+        const int l = k == 0 ? t.lx : (k == 1 ? t.ly : t.lz);
+        if (2 * g.d1[k] < (1LL << l)) return false;
+    }
     const long long ntx = (g.d1[0] + (1 << t.lx) - 1) >> t.lx;
     const long long nty = (g.d1[1] + (1 << t.ly) - 1) >> t.ly;
     const long long ntz = (g.d1[2] + (1 << t.lz) - 1) >> t.lz;
@@ -968,20 +1500,62 @@ bool tiled_supported(const LaunchArgs& a, const TileCfg& t) {
 }
 
 cudaError_t launch_pull_tiled(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s) {
-    const bool small = a.g.n0 < (1LL << 31) - 1;
+    const bool small = a.g.n0 < (1LL << 31) - 1 && a.g.n1 < (1LL << 31) - 1;
     switch (op) {
         case kPull: return small ? dispatch<kPull, int, false>(a, t, s) : dispatch<kPull, long long, false>(a, t, s);
         case kPullGrad:
             return small ? dispatch<kPullGrad, int, false>(a, t, s) : dispatch<kPullGrad, long long, false>(a, t, s);
-        default:
+        case kPullHess:
             return small ? dispatch<kPullHess, int, false>(a, t, s) : dispatch<kPullHess, long long, false>(a, t, s);
+        case kPullGradDot:
+            return small ? dispatch<kPullGradDot, int, false>(a, t, s)
+                         : dispatch<kPullGradDot, long long, false>(a, t, s);
+        default:
+            return small ? dispatch<kPullHessDot, int, false>(a, t, s)
+                         : dispatch<kPullHessDot, long long, false>(a, t, s);
     }
 }
 
 cudaError_t launch_push_tiled(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s) {
-    const bool small = a.g.n0 < (1LL << 31) - 1;
+    const bool small = a.g.n0 < (1LL << 31) - 1 && a.g.n1 < (1LL << 31) - 1;
     if (op == kPush) return small ? dispatch<kPush, int, true>(a, t, s) : dispatch<kPush, long long, true>(a, t, s);
     return small ? dispatch<kPushGrad, int, true>(a, t, s) : dispatch<kPushGrad, long long, true>(a, t, s);
+}
+
+int fused_tiled_grid(const LaunchArgs& a, const TileCfg& c) {
+    const TileGrid t = make_grid(a, c);
+    // two CTAs per SM: the shared memory (ring, box, accumulator) admits two
+    const long long want = 2LL * sm_count();
+    return (int)(t.ntiles < want ? t.ntiles : want);
+}
+
+cudaError_t launch_fused_tiled(const LaunchArgs& a, const TileCfg& t, cudaStream_t s, int grid) {
+    const bool small = a.g.n0 < (1LL << 31) - 1 && a.g.n1 < (1LL << 31) - 1;
+    switch (a.g.dp[0]) {
+        case 1: return small ? launch_fused_dp<1, int>(a, t, s, grid) : launch_fused_dp<1, long long>(a, t, s, grid);
+        case 2: return small ? launch_fused_dp<2, int>(a, t, s, grid) : launch_fused_dp<2, long long>(a, t, s, grid);
+        case 3: return small ? launch_fused_dp<3, int>(a, t, s, grid) : launch_fused_dp<3, long long>(a, t, s, grid);
+        case 4: return small ? launch_fused_dp<4, int>(a, t, s, grid) : launch_fused_dp<4, long long>(a, t, s, grid);
+        default: return small ? launch_fused_dp<5, int>(a, t, s, grid) : launch_fused_dp<5, long long>(a, t, s, grid);
+    }
+}
+
+TileGrid tile_grid(const LaunchArgs& a, const TileCfg& c) { return make_grid(a, c); }
+
+cudaError_t launch_batch(const BatchItem* items, int nitems, int total_tiles, unsigned* counter, int cap,
+                         cudaStream_t s) {
+    const size_t smem = (size_t)cap * sizeof(float);
+    cudaError_t e = opt_in(k_batch, smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kThreads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    const long long want = (long long)sm_count() * per_sm;
+    const int grid = (int)(total_tiles < want ? total_tiles : want);
+    if (grid < 1) return cudaSuccess;
+    k_batch<<<grid, kThreads, smem, s>>>(items, nitems, total_tiles, counter, cap);
+    return cudaGetLastError();
 }
 
 unsigned read_device_status(bool reset) {

@@ -28,6 +28,27 @@ struct TileGrid {
     int pmod;           // box row pitch P is chosen with P % 32 == pmod
 };
 
+// Fused forward + adjoint step over tiles: grid size for a launch, and the
+// launch itself (one loss partial per CTA into a.partial[0 .. grid)).
+int fused_tiled_grid(const LaunchArgs& a, const TileCfg& t);
+cudaError_t launch_fused_tiled(const LaunchArgs& a, const TileCfg& t, cudaStream_t s, int grid);
+
+// ---- batched uneven workload: one persistent launch over many volumes -------
+// One entry per (image, deformation) pair.  Every tile of every item is pulled
+// (f1 = pull(f0, phi), written) and the pulled values pushed back
+// (out += push(f1, phi)) by the CTA that owns the tile.
+struct BatchItem {
+    LaunchArgs pull;     // phi, in = f0, out = f1
+    LaunchArgs push;     // phi, in = f1, out = image-grid accumulator
+    TileGrid t;          // 512-voxel tiles
+    int tile_begin;      // first global tile index of this item
+    int dp;              // isotropic degree + 1
+};
+TileGrid tile_grid(const LaunchArgs& a, const TileCfg& c);
+// items in device memory; `counter` a zeroed device word for the work queue
+cudaError_t launch_batch(const BatchItem* items, int nitems, int total_tiles, unsigned* counter, int cap,
+                         cudaStream_t s);
+
 // Read (and optionally clear) the device status word of the current device:
 // bit 0 = a bounded device-side wait gave up.  0xffffffff if it cannot be read.
 unsigned read_device_status(bool reset);

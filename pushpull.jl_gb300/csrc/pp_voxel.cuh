@@ -18,20 +18,59 @@ __device__ __forceinline__ int bnd_code(const LaunchArgs& a, int c, int& b0, int
     return b0 | (b1 << 2) | (b2 << 4);
 }
 
+// output components per channel (dot ops: 3 for the whole voxel, see pull_out)
 template <int OP>
 __device__ __forceinline__ constexpr int pull_ncomp() {
-    return OP == kPull ? 1 : (OP == kPullGrad ? 3 : 9);
+    return OP == kPull ? 1 : (OP == kPullHess ? 9 : 3);
+}
+template <int OP>
+__device__ __forceinline__ constexpr bool pull_is_dot() {
+    return OP == kPullGradDot || OP == kPullHessDot;
+}
+// the contraction a pull-family op evaluates per channel
+template <int OP>
+__device__ __forceinline__ constexpr int pull_base_op() {
+    return OP == kPullGradDot ? kPullGrad : (OP == kPullHessDot ? kPullHess : OP);
+}
+// first output element of (batch b, channel c) for voxel v
+template <int OP>
+__device__ __forceinline__ float* pull_out(const LaunchArgs& a, int b, int c, long long v) {
+    constexpr int NCOMP = pull_ncomp<OP>();
+    if constexpr (pull_is_dot<OP>()) return a.out + (long long)b * 3 * a.g.n1 + v;
+    return a.out + ((long long)b * a.g.nc + c) * NCOMP * a.g.n1 + v;
 }
 
-// Write every component of every channel of voxel v as NaN (invalid sample).
+// Write every output component of voxel v as NaN (invalid sample).
 template <int OP>
 __device__ __forceinline__ void pull_voxel_nan(const LaunchArgs& a, int b, long long v) {
     constexpr int NCOMP = pull_ncomp<OP>();
     const long long n1 = a.g.n1;
-    float* outb = a.out + (long long)b * a.g.nc * NCOMP * n1 + v;
-    for (int c = 0; c < a.g.nc; ++c)
+    const int nch = pull_is_dot<OP>() ? 1 : a.g.nc;
+    for (int c = 0; c < nch; ++c) {
+        float* o = pull_out<OP>(a, b, c, v);
 #pragma unroll
-        for (int q = 0; q < NCOMP; ++q) outb[((long long)c * NCOMP + q) * n1] = qnan();
+        for (int q = 0; q < NCOMP; ++q) o[(long long)q * n1] = qnan();
+    }
+}
+
+// Accumulate one channel's gradient (r[0..2]) or Hessian (r[0..5] = xx, yy, zz,
+// xy, xz, yz) contracted with the upstream of (b, c, v) into acc[0..2].
+template <int OP>
+__device__ __forceinline__ void dot_accumulate(const LaunchArgs& a, int b, int c, long long v, const float (&r)[6],
+                                               float (&acc)[3]) {
+    const long long n1 = a.g.n1;
+    if constexpr (OP == kPullGradDot) {
+        const float u = __ldg(a.up + ((long long)b * a.g.nc + c) * n1 + v);
+        acc[0] = fmaf(u, r[0], acc[0]);
+        acc[1] = fmaf(u, r[1], acc[1]);
+        acc[2] = fmaf(u, r[2], acc[2]);
+    } else if constexpr (OP == kPullHessDot) {
+        const float* up = a.up + ((long long)b * a.g.nc + c) * 3 * n1 + v;
+        const float u0 = __ldg(up), u1 = __ldg(up + n1), u2 = __ldg(up + 2 * n1);
+        acc[0] += r[0] * u0 + r[3] * u1 + r[4] * u2;
+        acc[1] += r[3] * u0 + r[1] * u1 + r[5] * u2;
+        acc[2] += r[4] * u0 + r[5] * u1 + r[2] * u2;
+    }
 }
 
 // Store the per-op results of one channel (pull 1, grad 3, Hessian 9 planar comps).
@@ -58,7 +97,8 @@ __device__ __forceinline__ void pull_store(float* o, long long n1, const float (
 }
 
 // Separable patch contraction.  `tap(k, j, i)` returns the (signed) image value of
-// tap (i, j, k); weights come from the three axes.  Results in r[] as pull_store expects.
+// tap (i, j, k); weights come from the three axes.  Results in r[] as pull_store
+// expects; kPullValGrad returns the gradient in r[0..2] and the value in r[3].
 template <int OP, int N, class AX, class AY, class AZ, class TAP>
 __device__ __forceinline__ void contract(const AX& ax, const AY& ay, const AZ& az, int nx, int ny, int nz,
                                          bool runtime_n, TAP tap, float (&r)[6]) {
@@ -77,12 +117,12 @@ __device__ __forceinline__ void contract(const AX& ax, const AY& ay, const AZ& a
                 if (runtime_n && i >= nx) break;
                 const float f = tap(k, j, i);
                 i0 = fmaf(ax.w[i], f, i0);
-                if constexpr (OP >= kPullGrad) i1 = fmaf(ax.dw[i], f, i1);
-                if constexpr (OP >= kPullHess) i2 = fmaf(ax.hw[i], f, i2);
+                if constexpr (op_order(OP) >= 1) i1 = fmaf(ax.dw[i], f, i1);
+                if constexpr (op_order(OP) >= 2) i2 = fmaf(ax.hw[i], f, i2);
             }
             if constexpr (OP == kPull) {
                 j0 = fmaf(ay.w[j], i0, j0);
-            } else if constexpr (OP == kPullGrad) {
+            } else if constexpr (OP == kPullGrad || OP == kPullValGrad) {
                 j0 = fmaf(ay.w[j], i1, j0);    // d/dx
                 j1 = fmaf(ay.dw[j], i0, j1);   // d/dy
                 j2 = fmaf(ay.w[j], i0, j2);    // d/dz once the z derivative weight is applied
@@ -97,10 +137,11 @@ __device__ __forceinline__ void contract(const AX& ax, const AY& ay, const AZ& a
         }
         if constexpr (OP == kPull) {
             r[0] = fmaf(az.w[k], j0, r[0]);
-        } else if constexpr (OP == kPullGrad) {
+        } else if constexpr (OP == kPullGrad || OP == kPullValGrad) {
             r[0] = fmaf(az.w[k], j0, r[0]);
             r[1] = fmaf(az.w[k], j1, r[1]);
             r[2] = fmaf(az.dw[k], j2, r[2]);
+            if constexpr (OP == kPullValGrad) r[3] = fmaf(az.w[k], j2, r[3]);   // the value itself
         } else {
             r[0] = fmaf(az.w[k], j0, r[0]);
             r[1] = fmaf(az.w[k], j1, r[1]);
@@ -113,17 +154,17 @@ __device__ __forceinline__ void contract(const AX& ax, const AY& ay, const AZ& a
 }
 
 // pull family for one valid voxel, every channel, gathering from global memory.
-template <int DP, int OP, typename IT>
+template <int DP, int OP_, typename IT>
 __device__ __forceinline__ void pull_voxel_global(const LaunchArgs& a, int b, long long v, float x0, float x1,
                                                   float x2) {
-    constexpr int NCOMP = pull_ncomp<OP>();
+    constexpr int OP = pull_base_op<OP_>();
     const Geometry& g = a.g;
     const long long n1 = g.n1;
     const IT sy = (IT)g.d0[0];
     const IT sz = (IT)(g.d0[0] * g.d0[1]);
-    float* outb = a.out + (long long)b * g.nc * NCOMP * n1 + v;
-    Axis<DP, OP, IT> ax, ay, az;
-    constexpr int N = Axis<DP, OP, IT>::N;
+    float acc[3] = {0.f, 0.f, 0.f};
+    Axis<DP, op_order(OP), IT> ax, ay, az;
+    constexpr int N = Axis<DP, op_order(OP), IT>::N;
     int prev = -1;
     for (int c = 0; c < g.nc; ++c) {
         int b0, b1, b2;
@@ -138,7 +179,14 @@ __device__ __forceinline__ void pull_voxel_global(const LaunchArgs& a, int b, lo
         float r[6];
         contract<OP, N>(ax, ay, az, ax.n, ay.n, az.n, DP == 0,
                         [&](int k, int j, int i) { return __ldg(f0 + (az.off[k] + ay.off[j] + ax.off[i])); }, r);
-        pull_store<OP>(outb + (long long)c * NCOMP * n1, n1, r);
+        if constexpr (pull_is_dot<OP_>()) dot_accumulate<OP_>(a, b, c, v, r, acc);
+        else pull_store<OP>(pull_out<OP_>(a, b, c, v), n1, r);
+    }
+    if constexpr (pull_is_dot<OP_>()) {
+        float* o = pull_out<OP_>(a, b, 0, v);
+        o[0] = acc[0];
+        o[n1] = acc[1];
+        o[2 * n1] = acc[2];
     }
 }
 

@@ -116,3 +116,49 @@ def batched_pairs(seed: int = 4, npairs: int = 32, levels: int = 3):
             dl = tuple(max(1, (v + (1 << lev) - 1) >> lev) for v in d)
             items.append(dict(pair=p, level=lev, d=dl, channels=c, deg=deg, seed=seed * 1000 + p * 10 + lev))
     return items
+
+
+# ---- device-side generation (the batched workload has ~100 volumes) ---------
+def _smooth_gpu(vol, fwhm: float):
+    """Periodic Gaussian smoothing of a (X, Y, Z) float32 CUDA tensor by FFT."""
+    import torch
+    sigma = fwhm * FWHM_TO_SIGMA
+    F = torch.fft.rfftn(vol.double())
+    for ax, n in enumerate(vol.shape):
+        k = torch.fft.rfftfreq(n, device=vol.device) if ax == vol.dim() - 1 else torch.fft.fftfreq(n, device=vol.device)
+        h = torch.exp(-2.0 * (torch.pi * sigma * k.double()) ** 2)
+        shape = [1] * vol.dim()
+        shape[ax] = -1
+        F = F * h.view(shape)
+    return torch.fft.irfftn(F, s=vol.shape).float()
+
+
+def image_gpu(d, seed: int, fwhm: float = 3.0, channels: int = 1, device="cuda"):
+    """Column-major (d..., [C]) image: U(0,1) i.i.d. smoothed with FWHM ``fwhm``."""
+    import torch
+    from . import layout as L
+    g = torch.Generator(device=device).manual_seed(seed)
+    out = L.empty(tuple(d) + ((channels,) if channels > 1 else ()), device=device)
+    for c in range(channels):
+        v = torch.rand(tuple(d), generator=g, device=device)
+        sm = _smooth_gpu(v, fwhm)
+        if channels > 1:
+            out[..., c] = sm
+        else:
+            out.copy_(sm)
+    return out
+
+
+def deformation_gpu(d, seed: int, fwhm: float, amplitude: float, device="cuda"):
+    """Column-major (d..., 3): 1-based identity + smoothed N(0,1) field, max|u| = amplitude."""
+    import torch
+    from . import layout as L
+    g = torch.Generator(device=device).manual_seed(seed)
+    phi = L.empty(tuple(d) + (3,), device=device)
+    u = torch.stack([_smooth_gpu(torch.randn(tuple(d), generator=g, device=device), fwhm) for _ in range(3)], -1)
+    u *= amplitude / u.abs().max()
+    ax = [torch.arange(1, n + 1, dtype=torch.float32, device=device) for n in d]
+    phi[..., 0] = ax[0].view(-1, 1, 1) + u[..., 0]
+    phi[..., 1] = ax[1].view(1, -1, 1) + u[..., 1]
+    phi[..., 2] = ax[2].view(1, 1, -1) + u[..., 2]
+    return phi

@@ -32,7 +32,7 @@ def _phi(O, rng, d1, d0, sigma, nb=1):
 def restore_tiles(pkg):
     lib = pkg.native_library()
     saved = {}
-    for op in range(5):
+    for op in range(6):
         for d in range(5):
             v = [C.c_int() for _ in range(4)]
             assert lib.pp_get_tile(op, d, *[C.byref(x) for x in v]) == 0
@@ -120,3 +120,26 @@ def test_identity_reproduces_image(pkg, O):
     for deg in (0, 1):
         out = L.to_numpy(pkg.pull(L.from_numpy(f0), phi, pkg.Settings(deg, 1, 0)))
         assert np.array_equal(out, f0)
+
+
+def test_autotune_installs_valid_choice(pkg, O, restore_tiles, tmp_path, monkeypatch):
+    """The autotuner times candidates on the caller's arrays, installs a tile
+    configuration that still matches the oracle, and caches it."""
+    import importlib
+    A = importlib.import_module("pushpull_gb300.autotune")
+    monkeypatch.setattr(A, "CACHE", str(tmp_path / "tiles.json"))
+    L = pkg.layout
+    rng = np.random.default_rng(21)
+    d0 = d1 = (48, 40, 36)
+    f0 = np.asfortranarray(rng.standard_normal(d0).astype(np.float32))
+    phi = _phi(O, rng, d1, d0, 1.5)
+    s, so = pkg.Settings(3, 1, 1), O.Sett.make(3, 1, 1)
+    for op, x in [("pull", f0), ("push", f0)]:
+        res = A.tune(op, L.from_numpy(x), L.from_numpy(phi), s, d0=d0, reps=2)
+        assert res["path"] in ("tiled", "direct") and res["ms"] > 0
+        assert sum(res["tile"]) >= 6 and res["cap"] >= 4096
+    got1 = L.to_numpy(pkg.pull(L.from_numpy(f0), L.from_numpy(phi), s))
+    got0 = L.to_numpy(pkg.push(L.from_numpy(f0), L.from_numpy(phi), d0, s))
+    assert rel_err(got1, O.pull(f0, phi, so)) <= 1e-5
+    assert rel_err(got0, O.push(f0, phi, d0, so)) <= 1e-4
+    assert A.load() == sum(1 for v in __import__("json").load(open(A.CACHE)).values() if v["path"] == "tiled")
