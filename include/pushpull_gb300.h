@@ -130,6 +130,26 @@ int pp_fused_step(double *loss, float *df, float *dphi, const float *f0, const f
                   const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
                   const int *bnd, int nbnd, const int deg[3], int ext, int accumulate, void *stream);
 
+/* pp_fused_step for callers that must not allocate device memory.  No
+ * counterpart in the reference: it exists for programs whose own caching
+ * allocator already holds (nearly) all device memory, or whose request path
+ * forbids allocation, so a library allocating scratch would fail or fragment
+ * their pool.  Same arguments, results and errors as pp_fused_step; its
+ * scratch is an 80 KiB array compiled into the library (every device that
+ * loads the library keeps it until the process exits), so it calls no
+ * allocator.  Limits: at most PP_NOALLOC_MAX_PARTIALS loss partials (one per
+ * thread block: at most 1216 per batch element on 152 SMs) and at most
+ * PP_NOALLOC_MAX_PLANES planes nc * nb; beyond them it returns
+ * PP_ERR_TOO_LARGE without launching.  The first call on each device looks up
+ * the array's device address, so make it before any stream capture.  All calls
+ * share the one array: calls that overlap on the GPU (different streams or
+ * host threads without ordering between them) race and give wrong losses. */
+#define PP_NOALLOC_MAX_PARTIALS 8192
+#define PP_NOALLOC_MAX_PLANES 4096
+int pp_fused_step_noalloc(double *loss, float *df, float *dphi, const float *f0, const float *phi,
+                          const float *g, const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
+                          const int *bnd, int nbnd, const int deg[3], int ext, int accumulate, void *stream);
+
 /* ---- batched uneven workload ------------------------------------------- */
 /* One (image, deformation) pair of a batch: f1 = pull(f0, phi) is written and
  * out (+)= push(f1, phi) is accumulated, all device pointers, single batch,
