@@ -44,13 +44,9 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _traffic(name):
-    p = os.path.join(ROOT, "profiles", "traffic.json")
-    try:
-        with open(p) as fh:
-            return json.load(fh).get(name)
-    except Exception:
-        return None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each kernel
+# on this workload, from one ncu capture (profiles/k_pull_tiled_192cubic.md, profiles/k_push_tiled_192cubic.md).
+TRAFFIC = {"pull": 129_179_904, "push": 152_983_808}
 
 
 class Clocks:
@@ -230,6 +226,19 @@ def run_gpu(args):
         wall = time.perf_counter() - t0
     if ws > 1:
         dist.barrier()
+    # pull_grad of the same image and deformation (outside the timed pull+push step)
+    g1 = L.empty(d1 + (3,), device=dev)
+    pg_ms = []
+    for i in range(max(args.steps, 5) + 3):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        pkg.pull_grad(f0, phi, s, out=g1)
+        e1.record()
+        torch.cuda.synchronize()
+        if i >= 3:
+            pg_ms.append(e0.elapsed_time(e1))
+    del g1
     pull_ms = [e[0].elapsed_time(e[1]) for e in evs]
     push_ms = [e[1].elapsed_time(e[2]) for e in evs]
     step_ms = statistics.mean(a + b for a, b in zip(pull_ms, push_ms))
@@ -278,6 +287,8 @@ def run_gpu(args):
                "path": "host-pointer ABI pull() then push() (artifacts/C/pushpull.h signatures)"}
 
     fused = None if args.no_fused else fused_vs_plain(pkg, dev, args)
+    batched = None if args.no_batch else batched_leg(pkg, dev, args)
+    contention = None if args.no_contention else contention_leg(pkg, dev, args)
 
     if rank != 0:
         if ws > 1:
@@ -292,7 +303,7 @@ def run_gpu(args):
     ach = dom_bytes / (dom_ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
             "frac": ach / peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-            "algorithmic_bytes_per_launch": dom_bytes, "traffic": _traffic(dom)}
+            "algorithmic_bytes_per_launch": dom_bytes, "traffic": TRAFFIC.get(dom)}
     kernels = {
         "pull": {"ms": mp, "GB_s": bytes_pull / (mp * 1e-3) / 1e9, "frac_of_peak": bytes_pull / (mp * 1e-3) / 1e9 / peak,
                  "Gvox_s": n1 / (mp * 1e-3) / 1e9},
@@ -300,6 +311,14 @@ def run_gpu(args):
                  "Gvox_s": n1 / (mq * 1e-3) / 1e9},
         "pull+push_frac_of_peak": (bytes_pull + bytes_push) / ((mp + mq) * 1e-3) / 1e9 / peak,
     }
+    mg = statistics.median(pg_ms)
+    bytes_pg = 12 * n1 + 4 * nc * n0 + 12 * nc * n1
+    kernels["pull_grad"] = {"ms": mg, "GB_s": bytes_pg / (mg * 1e-3) / 1e9,
+                            "frac_of_peak": bytes_pg / (mg * 1e-3) / 1e9 / peak, "Gvox_s": n1 / (mg * 1e-3) / 1e9}
+    for k in ("pull", "push", "pull_grad"):
+        kernels[k]["traffic_bytes_ncu"] = TRAFFIC.get(k)
+    kernels["bytes_model"] = ("algorithmic bytes per launch: pull 12 n1 (phi) + 4 n0 (image, once) + 4 n1 (out); "
+                              "push 12 n1 + 4 n1 (values) + 4 n0 (image written once); pull_grad 12 n1 + 4 n0 + 12 n1")
     cpu = None
     if not args.no_cpu and ws == 1 or (not args.no_cpu and rank == 0):
         cpu, _ = cpu_baseline(w, seconds=args.cpu_seconds)
@@ -308,7 +327,8 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded): smoothed U(0,1) image, smoothed "
             "random displacement", "config": _config(w, args), "roofline": roof, "cpu_baseline": cpu,
             "e2e": e2e, "gpu_launches": 2 * args.steps, "clocks": clk.summary(), "kernels": kernels,
-            "fused_step": fused, "wall_s_timed_region": wall}
+            "fused_step": fused, "batched": batched, "contention_push": contention,
+            "wall_s_timed_region": wall}
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
@@ -382,6 +402,102 @@ def fused_vs_plain(pkg, dev, args):
             "accuracy_vs_fp64": "checked in tests/test_gpu_full.py at this size (<= 1e-4 relative)"}
 
 
+def _timeit(fn, reps, flush):
+    import torch
+    for _ in range(3):
+        fn()
+    ms = []
+    for _ in range(reps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return statistics.median(ms)
+
+
+def batched_leg(pkg, dev, args):
+    """Uneven batch: 32 pairs with sizes from 64^3 to 256x256x192, 1-3 channels,
+    degrees from {1,2,3}, each with a 3-level pyramid (96 volumes); pull then push
+    of every volume in one persistent launch replayed from a CUDA graph, against
+    one pull and one push call per volume."""
+    import torch
+    from pushpull_gb300 import batch as B
+    from pushpull_gb300 import workloads as W
+    L = pkg.layout
+    specs = W.batched_pairs(seed=4, npairs=32, levels=3)
+    items = []
+    vox = 0
+    for sp in specs:
+        d, c = sp["d"], sp["channels"]
+        f0 = W.image_gpu(d, sp["seed"], fwhm=3.0, channels=c, device=dev)
+        phi = W.deformation_gpu(d, sp["seed"] + 7, fwhm=8.0, amplitude=3.0 / (1 << sp["level"]), device=dev)
+        f1 = L.empty(tuple(d) + ((c,) if c > 1 else ()), device=dev)
+        out = L.empty(tuple(f0.shape), device=dev)
+        items.append(dict(f0=f0, phi=phi, f1=f1, out=out, sett=pkg.Settings(sp["deg"], 1, 1)))
+        vox += int(np.prod(d)) * c
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    plan = B.BatchPlan(items, zero_outputs=True)
+    with torch.cuda.stream(stream):
+        plan.capture(stream)
+    torch.cuda.synchronize()
+
+    def graph():
+        stream.wait_stream(torch.cuda.current_stream())
+        plan.launch(stream)
+        torch.cuda.current_stream().wait_stream(stream)
+
+    def per_item():
+        for it in items:
+            pkg.pull(it["f0"], it["phi"], it["sett"], out=it["f1"])
+            pkg.push(it["f1"], it["phi"], tuple(it["f0"].shape[:3]), it["sett"], out=it["out"], accumulate=False)
+
+    reps = max(min(args.steps, 10), 3)
+    t_graph = _timeit(graph, reps, flush)
+    t_items = _timeit(per_item, reps, flush)
+    tiles = plan.tiles
+    plan.close()
+    return {"workload": "32 pairs x 3 pyramid levels (96 volumes), sizes U[64,256]x[64,256]x[64,192] halved per "
+                        "level, 1-3 channels, degree from {1,2,3}, DCT-II, ext=1; pull then push each",
+            "voxels_x_channels": vox, "tiles": tiles, "graph_ms": t_graph, "per_item_ms": t_items,
+            "graph_Gvox_s": vox / (t_graph * 1e-3) / 1e9, "per_item_Gvox_s": vox / (t_items * 1e-3) / 1e9,
+            "speedup_vs_per_item": t_items / t_graph,
+            "launches": {"graph": 1, "per_item": 2 * len(items)}}
+
+
+def contention_leg(pkg, dev, args):
+    """Many-to-one scatter: 256^3 x 3 channels, cubic, DCT-II, deformation = 0.25x
+    contraction about the centre + FWHM-12 field of +-3 vox; push and push_grad."""
+    import torch
+    from pushpull_gb300 import workloads as W
+    L = pkg.layout
+    d = (256, 256, 256)
+    s = pkg.Settings(3, 1, 1)
+    f1 = W.image_gpu(d, 51, fwhm=3.0, channels=3, device=dev)
+    g1 = L.empty(d + (3, 3), device=dev)
+    g1.copy_(torch.randn(g1.shape, generator=torch.Generator(device=dev).manual_seed(52), device=dev))
+    phi = W.deformation_gpu(d, 53, fwhm=12.0, amplitude=3.0, contraction=0.25, device=dev)
+    out = L.empty(d + (3,), device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    reps = max(min(args.steps, 10), 3)
+    t_push = _timeit(lambda: pkg.push(f1, phi, d, s, out=out, accumulate=False), reps, flush)
+    t_pushg = _timeit(lambda: pkg.push_grad(g1, phi, d, s, out=out, accumulate=False), reps, flush)
+    n1, nc = int(np.prod(d)), 3
+    taps = 64
+    return {"workload": "push and push_grad, 256^3 x 3 channels Float32, cubic, DCT-II, ext=1, phi = 0.25x "
+                        "contraction about the centre + FWHM-12 field +-3 vox (source occupies ~1/64 of the grid)",
+            "push_ms": t_push, "push_grad_ms": t_pushg,
+            "push_Gvox_s": n1 * nc / (t_push * 1e-3) / 1e9, "push_grad_Gvox_s": n1 * nc / (t_pushg * 1e-3) / 1e9,
+            "scatter_updates_per_s": {"push": n1 * nc * taps / (t_push * 1e-3),
+                                      "push_grad": n1 * nc * taps / (t_pushg * 1e-3)},
+            "note": "scatter updates = voxels x channels x 64 taps, accumulated in shared memory as fixed-point "
+                    "integers (privatised) and flushed to HBM once per box word",
+            "accuracy_vs_fp64": "tests/test_gpu_full.py::test_c5_contention_push_vs_oracle"}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -393,6 +509,8 @@ def main(argv=None):
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--no-fused", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-contention", action="store_true")
     args = ap.parse_args(argv)
     import __graft_entry__ as entry
     entry.package()

@@ -149,15 +149,17 @@ def image_gpu(d, seed: int, fwhm: float = 3.0, channels: int = 1, device="cuda")
     return out
 
 
-def deformation_gpu(d, seed: int, fwhm: float, amplitude: float, device="cuda"):
-    """Column-major (d..., 3): 1-based identity + smoothed N(0,1) field, max|u| = amplitude."""
+def deformation_gpu(d, seed: int, fwhm: float, amplitude: float, contraction: float = 1.0, device="cuda"):
+    """Column-major (d..., 3): 1-based identity (optionally scaled by
+    ``contraction`` about the volume centre) + smoothed N(0,1) field, max|u| = amplitude."""
     import torch
     from . import layout as L
     g = torch.Generator(device=device).manual_seed(seed)
     phi = L.empty(tuple(d) + (3,), device=device)
     u = torch.stack([_smooth_gpu(torch.randn(tuple(d), generator=g, device=device), fwhm) for _ in range(3)], -1)
     u *= amplitude / u.abs().max()
-    ax = [torch.arange(1, n + 1, dtype=torch.float32, device=device) for n in d]
+    ax = [0.5 * (n + 1) + contraction * (torch.arange(1, n + 1, dtype=torch.float32, device=device) - 0.5 * (n + 1))
+          for n in d]
     phi[..., 0] = ax[0].view(-1, 1, 1) + u[..., 0]
     phi[..., 1] = ax[1].view(1, -1, 1) + u[..., 1]
     phi[..., 2] = ax[2].view(1, 1, -1) + u[..., 2]
