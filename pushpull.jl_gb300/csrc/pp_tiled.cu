@@ -1,1485 +1,22 @@
-// pp_tiled.cu -- shared-memory tiled pull family and privatised push family.
-//
-// A CTA owns a TX x TY x TZ tile of sample voxels (power-of-two sides, up to
-// 256*V voxels for 256 threads).  It reads the tile's deformation once,
-// reduces the integer first taps to the tile's footprint box in the image
-//   [min o, max o + dp - 1]  per dimension,
-// and, when the box fits its shared-memory budget:
-//   pull:  stages the box once per channel -- boundary folding and the DST-II
-//          sign are applied while staging, so taps index the box directly with
-//          no per-tap modulo -- then evaluates every voxel from shared memory;
-//   push:  zeroes a box-sized accumulator, scatters every voxel's weighted taps
-//          into it with shared-memory atomics, then flushes the box to the
-//          image with one global reduction per non-zero element (4-wide vector
-//          reductions on aligned interior runs) instead of dp^3 global atomics
-//          per voxel.
-// Tiles whose footprint does not fit (large local expansion, far-out
-// coordinates) take the per-voxel global path for that tile only.
-//
-// Latency: each CTA is persistent and walks a sequence of tiles.  The
-// deformation of the next kStages tiles (and, for push, their channel-0 values)
-// streams into a ring of shared-memory slots with TMA bulk tensor copies that
-// complete on mbarriers, so several tiles' worth of HBM reads are in flight per
-// SM while the current tile computes.  Pull additionally stages the next tile's
-// image box with cp.async into a second buffer.
-//
-// Bank layout: lanes of a warp cover TX consecutive x of the tile and
-// 32/TX consecutive tile rows in y.  The box row pitch P is chosen with
-// P % 32 == TX % 32, so for a smooth deformation the rows of one warp land in
-// disjoint bank ranges (TX = 32: bank = x mod 32 in every row).
-//
-// Reference kernels replaced: pull_element / pullg_element / pullh_element /
-// push_element / pushg_element (artifacts/C/pushpull.cu:33-163); per-voxel math
-// pull1 / pullg1 / pullh1 / push1 / pushg1 (artifacts/C/pushpull_dev.cu:236-354).
-#include <climits>
-#include <cstring>
-#include <map>
-#include <mutex>
-#include <utility>
-
-#include <cuda.h>
-#include <cudaTypedefs.h>
-
-#include "pp_tiled.cuh"
-#include "pp_voxel.cuh"
+// pp_tiled.cu -- host side of the tiled kernels: support test, grid shape, dispatch to the
+// per-group translation units and the combined device status
+// (kernels and helpers: pp_tiled_impl.cuh).
+#include "pp_tiled_impl.cuh"
 
 namespace pp {
 
-// Device status word: bits record bounded waits that gave up (read and cleared
-// by pp_device_status).
-__device__ unsigned int g_device_status;
-
-namespace {
-
-constexpr int kThreads = 256;
-constexpr int kStages = 4;                 // tiles of the ring in flight per CTA
-constexpr unsigned kStatusWaitTimeout = 1u;
-constexpr int kClamp = 1 << 29;    // first taps are clamped to +-kClamp for the box reduction
-
-template <int DP, int ORD>
-struct W3 {
-    float w[DP];
-    float dw[ORD >= 1 ? DP : 1];
-    float hw[ORD >= 2 ? DP : 1];
-};
-
-struct Box {
-    int lo[3];      // minima of the first taps
-    int xo;         // x origin of the box in shared memory: lo[0] rounded down to a multiple of 4
-    int ext[3];     // box extent (x counted from xo)
-    int P, Q, size; // row pitch (P % 32 == pmod, P % 4 == 0), plane pitch (multiple of 32), floats
-    int mode;       // 0 no valid voxel, 1 shared memory, 2 per-voxel global fallback
-    int interior;   // bit k: the box lies inside the image along dimension k (no folding)
-    float S;        // block sum of the caller's per-thread value (push: bound on sum |contribution|)
-    int E;          // scale exponent of the fixed-point accumulator for S (see scale_exponent)
-};
-
-__device__ __forceinline__ int clamp_tap(long long o) {
-    return (int)(o < -kClamp ? -kClamp : (o > kClamp ? kClamp : o));
-}
-
-__device__ __forceinline__ int first_tap_i(float x, int DP) {
-    return clamp_tap((long long)ceilf(__fsub_rn(x, 0.5f * (float)DP)));
-}
-
-// Exponent E of the fixed-point accumulator scale for a bound S on the sum of
-// |contributions|: S < 2^E.  INT_MAX: nothing to accumulate (S == 0);
-// INT_MIN: S non-finite or outside the range the scale factors cover, so the
-// tile accumulates in float instead.
-__device__ __forceinline__ int scale_exponent(float S) {
-    if (S == 0.f) return INT_MAX;
-    if (!(S > 0.f) || !finitef(S)) return INT_MIN;
-    int E;
-    frexpf(S * 1.0009765625f, &E);
-    return (E < -80 || E > 100) ? INT_MIN : E;
-}
-
-// Block-wide reduction of the first-tap bounds into the footprint box.
-// `words` = shared-memory words needed per box element (1 for pull, 2 for push).
-// Also sums `ssum` over the block into box.S (fixed order) and sets box.E.
-template <int DP>
-__device__ __forceinline__ void reduce_box(int (&mn)[3], int (&mx)[3], const TileGrid& t, const Geometry& g,
-                                           int words, Box& box, int (&red)[8][7], float ssum = 0.f) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        mn[k] = __reduce_min_sync(0xffffffffu, mn[k]);
-        mx[k] = __reduce_max_sync(0xffffffffu, mx[k]);
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) ssum += __shfl_xor_sync(0xffffffffu, ssum, off);
-    if (lane == 0) {
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            red[warp][k] = mn[k];
-            red[warp][3 + k] = mx[k];
-        }
-        red[warp][6] = __float_as_int(ssum);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float S = 0.f;
-        for (int w = 0; w < kThreads / 32; ++w) S += __int_as_float(red[w][6]);
-        box.S = S;
-        box.E = scale_exponent(S);
-        int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
-#pragma unroll
-        for (int w = 0; w < kThreads / 32; ++w)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                lo[k] = min(lo[k], red[w][k]);
-                hi[k] = max(hi[k], red[w][3 + k]);
-            }
-        if (lo[0] > hi[0]) {
-            box.mode = 0;
-        } else {
-            const int xo = lo[0] & ~3;
-            long long e[3];
-            e[0] = (long long)hi[0] + DP - xo;
-            e[1] = (long long)hi[1] + DP - lo[1];
-            e[2] = (long long)hi[2] + DP - lo[2];
-            int interior = 0;
-            if (xo >= 0 && (long long)hi[0] + DP <= g.d0[0]) interior |= 1;
-            if (lo[1] >= 0 && (long long)hi[1] + DP <= g.d0[1]) interior |= 2;
-            if (lo[2] >= 0 && (long long)hi[2] + DP <= g.d0[2]) interior |= 4;
-            // P % 32 == pmod and Q % 32 == 0 keep the warp's rows and planes in
-            // disjoint banks; when that padding would not fit, pack tightly.
-            long long P = (e[0] + 3) & ~3LL;
-            long long Pp = P + (((t.pmod - (int)(P & 31)) + 32) & 31);
-            long long Q = (Pp * e[1] + 31) & ~31LL;
-            if (Q * e[2] * words <= t.cap) {
-                P = Pp;
-            } else {
-                Q = (P * e[1] + 3) & ~3LL;
-            }
-            const long long size = Q * e[2];
-            const bool fits = e[0] <= 4096 && e[1] <= 4096 && e[2] <= 4096 && size * words <= t.cap;
-            box.mode = fits ? 1 : 2;
-            box.lo[0] = lo[0];
-            box.lo[1] = lo[1];
-            box.lo[2] = lo[2];
-            box.xo = xo;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) box.ext[k] = fits ? (int)e[k] : 0;
-            box.P = fits ? (int)P : 0;
-            box.Q = fits ? (int)Q : 0;
-            box.size = fits ? (int)size : 0;
-            box.interior = interior;
-        }
-    }
-    __syncthreads();
-}
-
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
-}
-
-__device__ __forceinline__ void cp_async_wait_all() {
-    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
-}
-
-// Rows of the box are distributed over warps; within a warp a group of `lpr`
-// lanes (a power of two) shares a row.
-struct RowWalk {
-    int lg, sub, e0;   // lanes per row = 1 << lg
-    int ry, rz;        // this lane group's current row
-    int sy, sz;        // row step split into (y, z) parts
-    int ey;
-    __device__ __forceinline__ RowWalk(int items_per_row, int ey_) {
-        const int n = items_per_row < 1 ? 1 : (items_per_row > 32 ? 32 : items_per_row);
-        lg = 32 - __clz(n - 1);                       // ceil(log2 n)
-        const int lane = threadIdx.x & 31;
-        sub = lane >> lg;
-        e0 = lane & ((1 << lg) - 1);
-        ey = ey_;
-        const int first = (threadIdx.x >> 5) * (32 >> lg) + sub;
-        const int step = (kThreads / 32) * (32 >> lg);
-        rz = first / ey;
-        ry = first - rz * ey;
-        sz = step / ey;
-        sy = step - sz * ey;
-    }
-    __device__ __forceinline__ int lpr() const { return 1 << lg; }
-    __device__ __forceinline__ void next() {
-        ry += sy;
-        rz += sz;
-        if (ry >= ey) {
-            ry -= ey;
-            ++rz;
-        }
-    }
-};
-
-// Folded walk over the box: fn(sm_index, global_index, sign) once per element.
-template <typename IT, class FN>
-__device__ __forceinline__ void walk_box(const Box& box, const Geometry& g, int b0, int b1, int b2, FN fn) {
-    const int ex = box.ext[0], ey = box.ext[1], ez = box.ext[2];
-    RowWalk rw(ex, ey);
-    const IT sy = (IT)g.d0[0];
-    const IT sz = (IT)(g.d0[0] * g.d0[1]);
-    const bool xin = box.interior & 1, yin = box.interior & 2, zin = box.interior & 4;
-    for (; rw.rz < ez; rw.next()) {
-        const int rz = rw.rz, ry = rw.ry;
-        float sgy = 1.f, sgz = 1.f;
-        const IT gy = yin ? (IT)(box.lo[1] + ry) : (IT)fold_tap(b1, (long long)box.lo[1] + ry, g.d0[1], sgy);
-        const IT gz = zin ? (IT)(box.lo[2] + rz) : (IT)fold_tap(b2, (long long)box.lo[2] + rz, g.d0[2], sgz);
-        const IT rowg = gz * sz + gy * sy;
-        const int rsm = rz * box.Q + ry * box.P;
-        const float syz = sgy * sgz;
-        if (xin) {
-            const IT base = rowg + (IT)box.xo;
-            for (int e = rw.e0; e < ex; e += rw.lpr()) fn(rsm + e, base + (IT)e, syz);
-        } else {
-            for (int e = rw.e0; e < ex; e += rw.lpr()) {
-                float sgx;
-                const IT gx = (IT)fold_tap(b0, (long long)box.xo + e, g.d0[0], sgx);
-                fn(rsm + e, rowg + gx, syz * sgx);
-            }
-        }
-    }
-}
-
-// Stage one channel of the image box into shared memory: interior boxes of a
-// 16-byte aligned image with d0[0] % 4 == 0 copy whole 16-byte row chunks with
-// cp.async (no folding, all signs +1); other boxes fold and sign per element.
-template <typename IT>
-__device__ __forceinline__ void stage_box(const Box& box, const Geometry& g, int b0, int b1, int b2,
-                                          const float* f0, float* sm) {
-    if (box.interior == 7 && (g.d0[0] & 3) == 0 && (reinterpret_cast<uintptr_t>(f0) & 15) == 0) {
-        const int ey = box.ext[1], ez = box.ext[2];
-        const int n4 = (box.ext[0] + 3) >> 2;
-        RowWalk rw(n4, ey);
-        const IT sy = (IT)g.d0[0];
-        const IT sz = (IT)(g.d0[0] * g.d0[1]);
-        for (; rw.rz < ez; rw.next()) {
-            const int rz = rw.rz, ry = rw.ry;
-            const float* src = f0 + ((IT)(box.lo[2] + rz) * sz + (IT)(box.lo[1] + ry) * sy + (IT)box.xo);
-            float* dst = sm + (rz * box.Q + ry * box.P);
-            for (int ch = rw.e0; ch < n4; ch += rw.lpr()) cp_async16(dst + 4 * ch, src + 4 * ch);
-        }
-        cp_async_wait_all();
-        return;
-    }
-    walk_box<IT>(box, g, b0, b1, b2, [&](int si, IT gi, float s) { sm[si] = s * __ldg(f0 + gi); });
-}
-
-// ---- push accumulation -----------------------------------------------------
-// Each box element holds two int32 words (hi, lo) of a fixed-point sum.  With
-// S >= the sum of |contribution| over the tile's channel (B-spline weights are
-// non-negative and sum to one per axis; derivative weights sum to at most 2 in
-// absolute value) and S < 2^E, a contribution c is split as
-//     c = hi * q1 + lo * q2 + rounding,  q1 = 2^(E-22), q2 = 2^(E-43),
-// |hi| <= 2^22 and |lo| <= 2^20, so 512 contributions per element cannot
-// overflow and the rounding error per element is at most 2^(E-35), i.e.
-// below 3e-11 of S.  Both words use native integer shared atomics.  Where E
-// is out of range (S = 0, non-finite, or extreme) the tile uses float atomics.
-constexpr float kMagic = 12582912.0f;     // 1.5 * 2^23: float -> nearest int for |y| <= 2^22
-constexpr int kMagicBits = 0x4B400000;
-
-__device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }   // -126 <= k <= 127
-
-struct FixedScale {
-    float inv_q1, q1, inv_q2, q2;
-    __device__ __forceinline__ void set(int E) {
-        inv_q1 = pow2f(22 - E);
-        q1 = pow2f(E - 22);
-        inv_q2 = pow2f(43 - E);
-        q2 = pow2f(E - 43);
-    }
-};
-
-// hi_addr / lo_addr: shared-window byte addresses of the element's two words
-__device__ __forceinline__ void fixed_add(unsigned hi_addr, unsigned lo_addr, float c, const FixedScale& fs) {
-    const float t1 = __fadd_rn(c * fs.inv_q1, kMagic);
-    const int h = __float_as_int(t1) - kMagicBits;
-    const float r = fmaf(-__fsub_rn(t1, kMagic), fs.q1, c);
-    const int l = __float_as_int(__fadd_rn(r * fs.inv_q2, kMagic)) - kMagicBits;
-    red_shared_s32(hi_addr, h);
-    red_shared_s32(lo_addr, l);
-}
-
-__device__ __forceinline__ float fixed_value(int h, int l, const FixedScale& fs) {
-    return fmaf(__int2float_rn(h), fs.q1, __int2float_rn(l) * fs.q2);
-}
-
-// Flush one channel's accumulator box into the image with global reductions:
-// interior rows of an aligned image use 4-wide vector reductions on aligned
-// groups, all-zero groups are skipped.  `val(si)` reads box element si.
-template <typename IT, class VAL>
-__device__ __forceinline__ void flush_box(const Box& box, const Geometry& g, int b0, int b1, int b2, float* f0,
-                                          VAL val) {
-    if ((box.interior & 1) && (g.d0[0] & 3) == 0 && (reinterpret_cast<uintptr_t>(f0) & 15) == 0) {
-        const int ey = box.ext[1], ez = box.ext[2];
-        const int n4 = (box.ext[0] + 3) >> 2;        // rows start at xo (16-byte aligned); whole groups
-        RowWalk rw(n4, ey);
-        const IT sy = (IT)g.d0[0];
-        const IT sz = (IT)(g.d0[0] * g.d0[1]);
-        for (; rw.rz < ez; rw.next()) {
-            const int rz = rw.rz, ry = rw.ry;
-            float sgy = 1.f, sgz = 1.f;
-            const IT gy = (box.interior & 2) ? (IT)(box.lo[1] + ry)
-                                             : (IT)fold_tap(b1, (long long)box.lo[1] + ry, g.d0[1], sgy);
-            const IT gz = (box.interior & 4) ? (IT)(box.lo[2] + rz)
-                                             : (IT)fold_tap(b2, (long long)box.lo[2] + rz, g.d0[2], sgz);
-            const float s = sgy * sgz;
-            float* grow = f0 + (gz * sz + gy * sy + (IT)box.xo);
-            const int rsm = rz * box.Q + ry * box.P;
-            for (int ch = rw.e0; ch < n4; ch += rw.lpr()) {
-                const int e = 4 * ch;
-                // elements past the box row (e >= ext) are zero in the accumulator
-                const float4 v = make_float4(s * val(rsm + e), s * val(rsm + e + 1), s * val(rsm + e + 2),
-                                             s * val(rsm + e + 3));
-                if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f)
-                    atomicAdd(reinterpret_cast<float4*>(grow + e), v);
-            }
-        }
-        return;
-    }
-    walk_box<IT>(box, g, b0, b1, b2, [&](int si, IT gi, float s) {
-        const float v = val(si);
-        if (v != 0.f) atomicAdd(f0 + gi, s * v);
-    });
-}
-
-// ---- tiles -----------------------------------------------------------------
-struct TileOrigin {
-    int b;            // batch
-    int x0, y0, z0;   // first sample voxel of the tile
-};
-
-// linear tile index (x fastest, batch slowest) -> tile origin
-__device__ __forceinline__ TileOrigin tile_origin(const TileGrid& t, int T) {
-    const unsigned u = (unsigned)T;
-    const unsigned q1 = (unsigned)(((unsigned long long)u * t.mx) >> t.sx);
-    const unsigned q2 = (unsigned)(((unsigned long long)q1 * t.my) >> t.sy);
-    const unsigned q3 = (unsigned)(((unsigned long long)q2 * t.mz) >> t.sz);
-    TileOrigin r;
-    r.x0 = (int)(u - q1 * (unsigned)t.ntx) << t.lx;
-    r.y0 = (int)(q1 - q2 * (unsigned)t.nty) << t.ly;
-    r.z0 = (int)(q2 - q3 * (unsigned)t.ntz) << t.lz;
-    r.b = (int)q3;
-    return r;
-}
-
-// This thread's tile-local voxel coordinates (fixed for the kernel's lifetime)
-// and the sample-grid dimensions as 32-bit integers.
-template <int V>
-struct ThreadVox {
-    int vx[V], vy[V], vz[V];
-    int D0, D1, D2;
-    __device__ __forceinline__ ThreadVox(const TileGrid& t, const Geometry& g) {
-#pragma unroll
-        for (int q = 0; q < V; ++q) {
-            const int lin = threadIdx.x + q * kThreads;
-            vx[q] = lin & ((1 << t.lx) - 1);
-            vy[q] = (lin >> t.lx) & ((1 << t.ly) - 1);
-            vz[q] = lin >> (t.lx + t.ly);
-        }
-        D0 = (int)g.d1[0];
-        D1 = (int)g.d1[1];
-        D2 = (int)g.d1[2];
-    }
-    // linear sample index of voxel q within its batch, or -1 outside the grid
-    template <typename IT>
-    __device__ __forceinline__ IT index(const TileOrigin& o, int q) const {
-        const int gx = o.x0 + vx[q], gy = o.y0 + vy[q], gz = o.z0 + vz[q];
-        if (gx >= D0 || gy >= D1 || gz >= D2) return (IT)-1;
-        return (IT)gx + (IT)D0 * ((IT)gy + (IT)D1 * (IT)gz);
-    }
-};
-
-template <int DP, int OP, typename IT>
-__device__ __noinline__ void pull_tile_fallback(const LaunchArgs& a, int b, long long v, float x0, float x1,
-                                                float x2) {
-    pull_voxel_global<DP, OP, IT>(a, b, v, x0, x1, x2);
-}
-
-template <int DP, int OP, typename IT>
-__device__ __noinline__ void push_tile_fallback(const LaunchArgs& a, int b, long long v, float x0, float x1,
-                                                float x2) {
-    push_voxel_global<DP, OP, IT>(a, b, v, x0, x1, x2);
-}
-
-// ---- tile ring: per-tile deformation (and push values) several tiles ahead ----
-//
-// Slot k of the ring holds one tile laid out as [component][z][y][x] -- exactly
-// the order of a 4-D TMA box (TX, TY, TZ, C) -- so the thread owning tile-local
-// voxel `lin` reads component k at slot + k*NV + lin.  With TMA, thread 0 fills
-// a slot with one bulk tensor copy per tensor that completes on the slot's
-// mbarrier; without it (unaligned geometry) the threads fill it with plain loads.
-
-__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait: gives up after kWaitCycles clock cycles, records the failure
-// in the device status word and returns false.
-constexpr long long kWaitCycles = 4000000000LL;   // about two seconds
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
-    if (mbar_try(bar, parity)) return true;
-    const long long t0 = clock64();
-    while (!mbar_try(bar, parity)) {
-        if (clock64() - t0 > kWaitCycles) {
-            atomicOr(&g_device_status, kStatusWaitTimeout);
-            return false;
-        }
-    }
-    return true;
-}
-__device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap* map, unsigned bar, int x, int y, int z,
-                                            int w) {
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
-        "%5}], [%6];" ::"r"(dst),
-        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(bar)
-        : "memory");
-}
-
-struct Ring {
-    float* base;       // first slot
-    int slot_floats;   // floats per slot
-    unsigned bars;     // shared address of the first mbarrier
-};
-
-// Fill ring slot (j % kStages) with tile T: deformation components 0..2 and
-// NVAL value components of channel 0 of `vals` (layout (d1, NVAL, nc, nb); the
-// push input, or the fused step's target).  Called by every thread.
-template <int V, int NVAL, bool TMA, typename IT>
-__device__ __forceinline__ void ring_fill(const Ring& r, int j, int T, const LaunchArgs& a, const TileGrid& t,
-                                          const ThreadVox<V>& tv, const CUtensorMap& phimap,
-                                          const CUtensorMap& valmap, const float* vals) {
-    constexpr int NV = kThreads * V;
-    float* slot = r.base + (j % kStages) * r.slot_floats;
-    const TileOrigin o = tile_origin(t, T);
-    if constexpr (TMA) {
-        if (threadIdx.x == 0) {
-            const unsigned bar = r.bars + 8u * (j % kStages);
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_expect_tx(bar, (unsigned)((3 + NVAL) * NV * sizeof(float)));
-            tma_load_4d(smem_addr(slot), &phimap, bar, o.x0, o.y0, o.z0, 3 * o.b);
-            if constexpr (NVAL > 0)
-                tma_load_4d(smem_addr(slot + 3 * NV), &valmap, bar, o.x0, o.y0, o.z0, NVAL * a.g.nc * o.b);
-        }
-    } else {
-        const long long n1 = a.g.n1;
-        const float* phi = a.phi + (long long)o.b * 3 * n1;
-        const float* val = vals + (long long)o.b * a.g.nc * NVAL * n1;
-#pragma unroll
-        for (int q = 0; q < V; ++q) {
-            const int lin = threadIdx.x + q * kThreads;
-            const IT v = tv.template index<IT>(o, q);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) slot[k * NV + lin] = v < 0 ? 0.f : __ldg(phi + v + k * n1);
-#pragma unroll
-            for (int k = 0; k < NVAL; ++k) slot[(3 + k) * NV + lin] = v < 0 ? 0.f : __ldg(val + v + k * n1);
-        }
-    }
-}
-
-template <bool TMA>
-__device__ __forceinline__ bool ring_wait(const Ring& r, int j) {
-    if constexpr (TMA) return mbar_wait(r.bars + 8u * (j % kStages), (unsigned)((j / kStages) & 1));
-    return true;
-}
-
-// First-tap bounds of this thread's valid voxels of the tile in `slot`.
-template <int DP, int V, typename IT>
-__device__ __forceinline__ void tile_bounds(const Geometry& g, const TileOrigin& o, const ThreadVox<V>& tv,
-                                            const float* slot, int (&mn)[3], int (&mx)[3]) {
-    constexpr int NV = kThreads * V;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        mn[k] = INT_MAX;
-        mx[k] = INT_MIN;
-    }
-#pragma unroll
-    for (int q = 0; q < V; ++q) {
-        const int lin = threadIdx.x + q * kThreads;
-        if (tv.template index<IT>(o, q) < 0) continue;
-        float x[3];
-        if (!load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x[0], x[1], x[2])) continue;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const int f = first_tap32(x[k], DP);
-            const int c = f < -kClamp ? -kClamp : (f > kClamp ? kClamp : f);
-            mn[k] = min(mn[k], c);
-            mx[k] = max(mx[k], c);
-        }
-    }
-}
-
-// Evaluate channel c of a tile for the pull family (dot ops accumulate into
-// acc[q] and store after the last channel).
-template <int DP, int OP_, int V, typename IT>
-__device__ __forceinline__ void pull_compute(const LaunchArgs& a, const TileOrigin& o, const ThreadVox<V>& tv,
-                                             const float* slot, int c, const Box& box, const float* sm,
-                                             float (&acc)[V][3]) {
-    constexpr int OP = pull_base_op<OP_>();
-    constexpr int NCOMP = pull_ncomp<OP_>();
-    constexpr int NV = kThreads * V;
-    const Geometry& g = a.g;
-    const long long n1 = g.n1;
-    const bool last = c == g.nc - 1;
-#pragma unroll
-    for (int q = 0; q < V; ++q) {
-        const IT v = tv.template index<IT>(o, q);
-        if (v < 0) continue;
-        const int lin = threadIdx.x + q * kThreads;
-        float x0, x1, x2;
-        if (!load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2)) {
-            if (!pull_is_dot<OP_>() || last) {
-                float* out = pull_out<OP_>(a, o.b, c, (long long)v);
-#pragma unroll
-                for (int p = 0; p < NCOMP; ++p) out[(long long)p * n1] = qnan();
-            }
-            continue;
-        }
-        if (box.mode != 1) {
-            if (c == 0) pull_tile_fallback<DP, OP_, IT>(a, o.b, (long long)v, x0, x1, x2);
-            continue;
-        }
-        constexpr int ORD = op_order(OP);
-        W3<DP, ORD> wx, wy, wz;
-        const int ox = spline_taps32<DP, ORD>(x0, wx.w, wx.dw, wx.hw) - box.xo;
-        const int oy = spline_taps32<DP, ORD>(x1, wy.w, wy.dw, wy.hw) - box.lo[1];
-        const int oz = spline_taps32<DP, ORD>(x2, wz.w, wz.dw, wz.hw) - box.lo[2];
-        const unsigned P4 = 4u * box.P, Q4 = 4u * box.Q;
-        const unsigned p = smem_addr(sm) + 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
-        float r[6];
-        contract<OP, DP>(wx, wy, wz, DP, DP, DP, false,
-                         [&](int k, int j, int i) { return lds_f32(p + k * Q4 + j * P4 + 4u * i); }, r);
-        if constexpr (pull_is_dot<OP_>()) {
-            dot_accumulate<OP_>(a, o.b, c, (long long)v, r, acc[q]);
-            if (last) {
-                float* out = pull_out<OP_>(a, o.b, 0, (long long)v);
-                out[0] = acc[q][0];
-                out[n1] = acc[q][1];
-                out[2 * n1] = acc[q][2];
-            }
-        } else {
-            pull_store<OP>(pull_out<OP_>(a, o.b, c, (long long)v), n1, r);
-        }
-    }
-}
-
-// Persistent, software-pipelined pull family.  CTA i walks tiles i, i+G, i+2G, ...
-// (G = grid size).  The deformation of the next kStages tiles is in flight in the
-// tile ring; while tile j is evaluated from one box buffer, the box of tile j+1
-// is being staged into the other with cp.async.
-template <int DP, int OP, int V, typename IT, bool TMA>
-__global__ void __launch_bounds__(kThreads, 2) k_pull_tiled(const __grid_constant__ LaunchArgs a,
-                                                            const __grid_constant__ TileGrid t,
-                                                            const __grid_constant__ CUtensorMap phimap) {
-    extern __shared__ __align__(128) float4 smem4[];
-    constexpr int NV = kThreads * V;
-    __shared__ int red[8][7];
-    __shared__ Box boxm[2];
-    __shared__ int s_abort;
-    const Geometry& g = a.g;
-    const int G = gridDim.x;
-    const int T0 = blockIdx.x;
-    if (T0 >= t.ntiles) return;
-    const int ntl = (t.ntiles - T0 + G - 1) / G;
-    const ThreadVox<V> tv(t, g);
-
-    float* sm = reinterpret_cast<float*>(smem4);
-    Ring ring;
-    ring.base = sm;
-    ring.slot_floats = 3 * NV;
-    float* bufs = sm + kStages * 3 * NV;
-    ring.bars = smem_addr(bufs + 2 * t.cap);
-    if (threadIdx.x == 0) {
-        s_abort = 0;
-        if (TMA) {
-            for (int k = 0; k < kStages; ++k) mbar_init(ring.bars + 8u * k, 1);
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        }
-    }
-    __syncthreads();
-    for (int j = 0; j < kStages && j < ntl; ++j)
-        ring_fill<V, 0, TMA, IT>(ring, j, T0 + j * G, a, t, tv, phimap, phimap, a.in);
-    if (!TMA) __syncthreads();
-
-    // box of tile j (its deformation must be in the ring), staged into buffer j & 1
-    auto prepare = [&](int j) {
-        const TileOrigin o = tile_origin(t, T0 + j * G);
-        const float* slot = ring.base + (j % kStages) * ring.slot_floats;
-        if (!ring_wait<TMA>(ring, j)) s_abort = 1;
-        int mn[3], mx[3];
-        tile_bounds<DP, V, IT>(g, o, tv, slot, mn, mx);
-        reduce_box<DP>(mn, mx, t, g, 1, boxm[j & 1], red);
-        if (boxm[j & 1].mode == 1) {
-            int b0, b1, b2;
-            bnd_code(a, 0, b0, b1, b2);
-            stage_box<IT>(boxm[j & 1], g, b0, b1, b2, a.in + (long long)o.b * g.nc * g.n0, bufs + (j & 1) * t.cap);
-        }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-    };
-
-    prepare(0);
-    for (int j = 0; j < ntl; ++j) {
-        if (j + 1 < ntl) {
-            prepare(j + 1);
-            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        }
-        __syncthreads();   // box j is in its buffer
-        if (s_abort) break;
-        const TileOrigin o = tile_origin(t, T0 + j * G);
-        const float* slot = ring.base + (j % kStages) * ring.slot_floats;
-        const Box& box = boxm[j & 1];
-        float* buf = bufs + (j & 1) * t.cap;
-        float acc[V][3];
-#pragma unroll
-        for (int q = 0; q < V; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.f;
-        pull_compute<DP, OP, V, IT>(a, o, tv, slot, 0, box, buf, acc);
-        for (int c = 1; c < g.nc; ++c) {
-            __syncthreads();   // channel c-1 reads of the buffer are done
-            if (box.mode == 1) {
-                int b0, b1, b2;
-                bnd_code(a, c, b0, b1, b2);
-                stage_box<IT>(box, g, b0, b1, b2, a.in + ((long long)o.b * g.nc + c) * g.n0, buf);
-                asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
-            }
-            __syncthreads();
-            pull_compute<DP, OP, V, IT>(a, o, tv, slot, c, box, buf, acc);
-        }
-        __syncthreads();   // ring slot j and buffer j & 1 are free
-        if (j + kStages < ntl)
-            ring_fill<V, 0, TMA, IT>(ring, j + kStages, T0 + (j + kStages) * G, a, t, tv, phimap, phimap, a.in);
-        if (!TMA) __syncthreads();
-    }
-}
-
-// Scatter one voxel into the push accumulator (box-relative first taps ox, oy, oz).
-// FIXED: two int32 words per element (values pre-scaled to q1 units); otherwise float.
-// WT: any weight set with w (and dw for push_grad) of DP taps.
-template <int DP, int OP, bool FIXED, class WT>
-__device__ __forceinline__ void push_scatter(const WT& wx, const WT& wy, const WT& wz, float v0, float v1, float v2,
-                                             unsigned base, unsigned P4, unsigned Q4, unsigned lo_off) {
-#pragma unroll
-    for (int k = 0; k < DP; ++k) {
-#pragma unroll
-        for (int j = 0; j < DP; ++j) {
-            float ca, cb;
-            if constexpr (OP == kPushGrad) {
-                ca = v0 * (wy.w[j] * wz.w[k]);
-                cb = v1 * (wy.dw[j] * wz.w[k]) + v2 * (wy.w[j] * wz.dw[k]);
-            } else {
-                ca = 0.f;
-                cb = v0 * (wy.w[j] * wz.w[k]);
-            }
-            const unsigned row = base + k * Q4 + j * P4;
-#pragma unroll
-            for (int i = 0; i < DP; ++i) {
-                float y;
-                if constexpr (OP == kPushGrad) y = fmaf(ca, wx.dw[i], cb * wx.w[i]);
-                else y = cb * wx.w[i];
-                if constexpr (FIXED) {
-                    // y in q1 units, |y| <= 2^22: hi = round(y), lo = round((y - hi) * 2^21)
-                    const float t1 = __fadd_rn(y, kMagic);
-                    const float r = __fsub_rn(y, __fsub_rn(t1, kMagic));
-                    const int h = __float_as_int(t1) - kMagicBits;
-                    const int l = __float_as_int(__fmaf_rn(r, 2097152.0f, kMagic)) - kMagicBits;
-                    red_shared_s32(row + 4u * i, h);
-                    red_shared_s32(row + lo_off + 4u * i, l);
-                } else {
-                    red_shared_f32(row + 4u * i, y);
-                }
-            }
-        }
-    }
-}
-
-// Persistent push family.  The ring holds each tile's deformation and its
-// channel-0 values kStages tiles ahead; the tile scatters into the shared
-// accumulator and flushes it with global reductions.  The flush clears every
-// element it reads, so the accumulator is zero again for the next tile.
-template <int DP, int OP, int V, typename IT, bool TMA>
-__global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constant__ LaunchArgs a,
-                                                            const __grid_constant__ TileGrid t,
-                                                            const __grid_constant__ CUtensorMap phimap,
-                                                            const __grid_constant__ CUtensorMap valmap) {
-    extern __shared__ __align__(128) float4 smem4[];
-    constexpr int ORD = OP == kPushGrad ? 1 : 0;
-    constexpr int NCOMP = OP == kPushGrad ? 3 : 1;
-    constexpr int NV = kThreads * V;
-    __shared__ int red[8][7];
-    __shared__ float sred[8];
-    __shared__ Box box;
-    __shared__ int s_abort;
-    const Geometry& g = a.g;
-    const long long n1 = g.n1;
-    const int G = gridDim.x;
-    const int T0 = blockIdx.x;
-    if (T0 >= t.ntiles) return;
-    const int ntl = (t.ntiles - T0 + G - 1) / G;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const ThreadVox<V> tv(t, g);
-
-    float* sm = reinterpret_cast<float*>(smem4);
-    Ring ring;
-    ring.base = sm;
-    ring.slot_floats = (3 + NCOMP) * NV;
-    float* accf = sm + kStages * (3 + NCOMP) * NV;
-    ring.bars = smem_addr(accf + t.cap);
-    for (int i = threadIdx.x; i < (t.cap >> 2); i += kThreads)
-        reinterpret_cast<float4*>(accf)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (threadIdx.x == 0) {
-        s_abort = 0;
-        if (TMA) {
-            for (int k = 0; k < kStages; ++k) mbar_init(ring.bars + 8u * k, 1);
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        }
-    }
-    __syncthreads();
-    for (int j = 0; j < kStages && j < ntl; ++j)
-        ring_fill<V, NCOMP, TMA, IT>(ring, j, T0 + j * G, a, t, tv, phimap, valmap, a.in);
-    if (!TMA) __syncthreads();
-
-    const unsigned acc_base = smem_addr(accf);
-    for (int j = 0; j < ntl; ++j) {
-        const TileOrigin o = tile_origin(t, T0 + j * G);
-        const float* slot = ring.base + (j % kStages) * ring.slot_floats;
-        if (!ring_wait<TMA>(ring, j)) s_abort = 1;
-        // deformation validity, first-tap bounds and the channel-0 scale bound
-        int mn[3], mx[3];
-        tile_bounds<DP, V, IT>(g, o, tv, slot, mn, mx);
-        float bound0 = 0.f;
-#pragma unroll
-        for (int q = 0; q < V; ++q) {
-            const int lin = threadIdx.x + q * kThreads;
-            float x0, x1, x2;
-            if (tv.template index<IT>(o, q) < 0 ||
-                !load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2))
-                continue;
-            bool fin = true;
-            float s1 = 0.f;
-#pragma unroll
-            for (int p = 0; p < NCOMP; ++p) {
-                const float v = slot[(3 + p) * NV + lin];
-                fin = fin && finitef(v);
-                s1 += fabsf(v);
-            }
-            if (fin) bound0 += OP == kPushGrad ? 2.f * s1 : s1;
-        }
-        reduce_box<DP>(mn, mx, t, g, 2, box, red, bound0);
-        if (s_abort) break;
-        if (box.mode == 2) {
-#pragma unroll
-            for (int q = 0; q < V; ++q) {
-                const IT v = tv.template index<IT>(o, q);
-                const int lin = threadIdx.x + q * kThreads;
-                float x0, x1, x2;
-                if (v >= 0 && load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2))
-                    push_tile_fallback<DP, OP, IT>(a, o.b, (long long)v, x0, x1, x2);
-            }
-        } else if (box.mode == 1) {
-            const unsigned lo_off = 4u * (unsigned)box.size;
-            int* acc_hi = reinterpret_cast<int*>(accf);
-            int* acc_lo = acc_hi + box.size;
-            const float* inb = a.in + (long long)o.b * g.nc * NCOMP * n1;
-            for (int c = 0; c < g.nc; ++c) {
-                int b0, b1, b2;
-                bnd_code(a, c, b0, b1, b2);
-                int E = box.E;
-                if (c > 0) {
-                    // values of channel c straight from global memory, and their scale bound
-                    float bound = 0.f;
-#pragma unroll
-                    for (int q = 0; q < V; ++q) {
-                        const IT v = tv.template index<IT>(o, q);
-                        const int lin = threadIdx.x + q * kThreads;
-                        float x0, x1, x2;
-                        if (v < 0 || !load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2))
-                            continue;
-                        bool fin = true;
-                        float s1 = 0.f;
-#pragma unroll
-                        for (int p = 0; p < NCOMP; ++p) {
-                            const float vv = __ldg(inb + (long long)c * NCOMP * n1 + v + p * n1);
-                            fin = fin && finitef(vv);
-                            s1 += fabsf(vv);
-                        }
-                        if (fin) bound += OP == kPushGrad ? 2.f * s1 : s1;
-                    }
-#pragma unroll
-                    for (int off = 16; off > 0; off >>= 1) bound += __shfl_xor_sync(0xffffffffu, bound, off);
-                    __syncthreads();   // the previous channel's flush is done
-                    if (lane == 0) sred[warp] = bound;
-                    __syncthreads();
-                    float S = 0.f;
-                    for (int w = 0; w < kThreads / 32; ++w) S += sred[w];
-                    E = scale_exponent(S);
-                }
-                if (E == INT_MAX) continue;   // every value of this channel is zero or skipped
-                const bool fixed = E != INT_MIN;
-                FixedScale fs;
-                fs.set(fixed ? E : 0);
-#pragma unroll
-                for (int q = 0; q < V; ++q) {
-                    const IT v = tv.template index<IT>(o, q);
-                    const int lin = threadIdx.x + q * kThreads;
-                    float x0, x1, x2;
-                    if (v < 0 || !load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2)) continue;
-                    float val[NCOMP];
-                    bool fin = true;
-#pragma unroll
-                    for (int p = 0; p < NCOMP; ++p) {
-                        val[p] = c == 0 ? slot[(3 + p) * NV + lin] : __ldg(inb + (long long)c * NCOMP * n1 + v + p * n1);
-                        fin = fin && finitef(val[p]);
-                    }
-                    if (!fin) continue;
-                    W3<DP, ORD> wx, wy, wz;
-                    const int ox = spline_taps32<DP, ORD>(x0, wx.w, wx.dw, wx.hw) - box.xo;
-                    const int oy = spline_taps32<DP, ORD>(x1, wy.w, wy.dw, wy.hw) - box.lo[1];
-                    const int oz = spline_taps32<DP, ORD>(x2, wz.w, wz.dw, wz.hw) - box.lo[2];
-                    const unsigned P4 = 4u * box.P, Q4 = 4u * box.Q;
-                    const unsigned base = acc_base + 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
-                    const float sc = fixed ? fs.inv_q1 : 1.f;
-                    const float w0 = val[0] * sc;
-                    const float w1 = NCOMP > 1 ? val[NCOMP > 1 ? 1 : 0] * sc : 0.f;
-                    const float w2 = NCOMP > 2 ? val[NCOMP > 2 ? 2 : 0] * sc : 0.f;
-                    if (fixed) push_scatter<DP, OP, true>(wx, wy, wz, w0, w1, w2, base, P4, Q4, lo_off);
-                    else push_scatter<DP, OP, false>(wx, wy, wz, w0, w1, w2, base, P4, Q4, lo_off);
-                }
-                __syncthreads();   // the scatter is complete
-                float* f0 = a.out + ((long long)o.b * g.nc + c) * g.n0;
-                if (fixed)
-                    flush_box<IT>(box, g, b0, b1, b2, f0, [&](int si) {
-                        const float v = fixed_value(acc_hi[si], acc_lo[si], fs);
-                        acc_hi[si] = 0;
-                        acc_lo[si] = 0;
-                        return v;
-                    });
-                else
-                    flush_box<IT>(box, g, b0, b1, b2, f0, [&](int si) {
-                        const float v = accf[si];
-                        accf[si] = 0.f;
-                        return v;
-                    });
-            }
-        }
-        __syncthreads();   // ring slot j is free and the accumulator is clear
-        if (j + kStages < ntl)
-            ring_fill<V, NCOMP, TMA, IT>(ring, j + kStages, T0 + (j + kStages) * G, a, t, tv, phimap, valmap, a.in);
-        if (!TMA) __syncthreads();
-    }
-}
-
-// ---- fused forward + adjoint step ------------------------------------------
-//
-// loss = sum_{b,c,v} (pull(f_c, phi)[v] - g_c[v])^2, df = push(2 r), and
-// dphi[v] = sum_c 2 r_c grad pull(f_c)[v]: the forward pull, the pull rrule's
-// two cotangents (src/pushpull_pb.jl:11-18) and the loss of the differentiable
-// step in one pass.  The image box is staged once per (tile, channel) and serves
-// both the value and the gradient; delta = 2 r is scattered into the shared
-// accumulator of the same box and flushed with global reductions.
-
-// Per-voxel global-memory version of one channel (tiles whose box does not fit):
-// returns the residual r and the gradient; scatters 2 r into df with atomics.
-template <int DP, typename IT>
-__device__ __noinline__ float fused_voxel_global(const LaunchArgs& a, int b, int c, long long v, float x0, float x1,
-                                                 float x2, float gv, float (&grad)[3]) {
-    const Geometry& g = a.g;
-    const IT sy = (IT)g.d0[0];
-    const IT sz = (IT)(g.d0[0] * g.d0[1]);
-    int b0, b1, b2;
-    bnd_code(a, c, b0, b1, b2);
-    Axis<DP, 1, IT> ax, ay, az;
-    ax.setup(x0, g.dp[0], b0, g.d0[0], (IT)1);
-    ay.setup(x1, g.dp[1], b1, g.d0[1], sy);
-    az.setup(x2, g.dp[2], b2, g.d0[2], sz);
-    const float* f0 = a.in + ((long long)b * g.nc + c) * g.n0;
-    float r[6];
-    contract<kPullValGrad, DP>(ax, ay, az, DP, DP, DP, false,
-                               [&](int k, int j, int i) { return __ldg(f0 + (az.off[k] + ay.off[j] + ax.off[i])); }, r);
-    grad[0] = r[0];
-    grad[1] = r[1];
-    grad[2] = r[2];
-    const float res = r[3] - gv;
-    const float d = 2.f * res;
-    if (finitef(d)) {
-        float* df = a.out + ((long long)b * g.nc + c) * g.n0;
-#pragma unroll
-        for (int k = 0; k < DP; ++k)
-#pragma unroll
-            for (int j = 0; j < DP; ++j) {
-                const float cb = d * (ay.w[j] * az.w[k]);
-#pragma unroll
-                for (int i = 0; i < DP; ++i) atomicAdd(df + (az.off[k] + ay.off[j] + ax.off[i]), cb * ax.w[i]);
-            }
-    }
-    return res;
-}
-
-template <int DP, int V, typename IT, bool TMA>
-__global__ void __launch_bounds__(kThreads, 2) k_fused_tiled(const __grid_constant__ LaunchArgs a,
-                                                             const __grid_constant__ TileGrid t,
-                                                             const __grid_constant__ CUtensorMap phimap,
-                                                             const __grid_constant__ CUtensorMap gmap) {
-    extern __shared__ __align__(128) float4 smem4[];
-    constexpr int NV = kThreads * V;
-    __shared__ int red[8][7];
-    __shared__ float sred[8];
-    __shared__ double dred[8];
-    __shared__ Box boxm[2];
-    __shared__ int s_abort;
-    const Geometry& g = a.g;
-    const long long n1 = g.n1;
-    const int G = gridDim.x;
-    const int T0 = blockIdx.x;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int ntl = T0 < t.ntiles ? (t.ntiles - T0 + G - 1) / G : 0;
-    const ThreadVox<V> tv(t, g);
-    double loss = 0.0;
-
-    float* sm = reinterpret_cast<float*>(smem4);
-    Ring ring;
-    ring.base = sm;
-    ring.slot_floats = 4 * NV;                       // deformation + channel-0 target
-    float* bufs = sm + kStages * 4 * NV;              // image box, double buffered
-    float* accf = bufs + 2 * t.cap;                   // adjoint accumulator: 2 words per element
-    ring.bars = smem_addr(accf + 2 * t.cap);
-    for (int i = threadIdx.x; i < (2 * t.cap) >> 2; i += kThreads)
-        reinterpret_cast<float4*>(accf)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (threadIdx.x == 0) {
-        s_abort = 0;
-        if (TMA) {
-            for (int k = 0; k < kStages; ++k) mbar_init(ring.bars + 8u * k, 1);
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        }
-    }
-    __syncthreads();
-    for (int j = 0; j < kStages && j < ntl; ++j)
-        ring_fill<V, 1, TMA, IT>(ring, j, T0 + j * G, a, t, tv, phimap, gmap, a.up);
-    if (!TMA) __syncthreads();
-
-    // Box of tile j and the channel-0 scale bound: |r| <= max|f| + |g| because the
-    // B-spline weights are non-negative and sum to one, so the sum of |2 r w|
-    // over a voxel's taps is at most 2 (max|f| + |g|).
-    auto prepare = [&](int j) {
-        const TileOrigin o = tile_origin(t, T0 + j * G);
-        const float* slot = ring.base + (j % kStages) * ring.slot_floats;
-        if (!ring_wait<TMA>(ring, j)) s_abort = 1;
-        int mn[3], mx[3];
-        tile_bounds<DP, V, IT>(g, o, tv, slot, mn, mx);
-        const float M = __uint_as_float(a.fmax[(long long)o.b * g.nc]);
-        float bound = 0.f;
-#pragma unroll
-        for (int q = 0; q < V; ++q) {
-            const int lin = threadIdx.x + q * kThreads;
-            float x0, x1, x2;
-            if (tv.template index<IT>(o, q) >= 0 &&
-                load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2))
-                bound += 2.f * (M + fabsf(slot[3 * NV + lin]));
-        }
-        reduce_box<DP>(mn, mx, t, g, 1, boxm[j & 1], red, bound);
-        if (boxm[j & 1].mode == 1) {
-            int b0, b1, b2;
-            bnd_code(a, 0, b0, b1, b2);
-            stage_box<IT>(boxm[j & 1], g, b0, b1, b2, a.in + (long long)o.b * g.nc * g.n0, bufs + (j & 1) * t.cap);
-        }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-    };
-
-    if (ntl > 0) prepare(0);
-    const unsigned acc_base = smem_addr(accf);
-    int* acc_hi = reinterpret_cast<int*>(accf);
-    for (int j = 0; j < ntl; ++j) {
-        if (j + 1 < ntl) {
-            prepare(j + 1);
-            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        }
-        __syncthreads();   // box j is in its buffer
-        if (s_abort) break;
-        const TileOrigin o = tile_origin(t, T0 + j * G);
-        const float* slot = ring.base + (j % kStages) * ring.slot_floats;
-        const Box& box = boxm[j & 1];
-        float* buf = bufs + (j & 1) * t.cap;
-        const unsigned lo_off = 4u * (unsigned)box.size;
-        int* acc_lo = acc_hi + box.size;
-        float dphi[V][3];
-        unsigned valid = 0;
-#pragma unroll
-        for (int q = 0; q < V; ++q) dphi[q][0] = dphi[q][1] = dphi[q][2] = 0.f;
-        for (int c = 0; c < g.nc; ++c) {
-            int b0, b1, b2;
-            bnd_code(a, c, b0, b1, b2);
-            const float* gc = a.up + ((long long)o.b * g.nc + c) * n1;
-            int E = box.E;
-            if (c > 0) {
-                __syncthreads();   // channel c-1 is done with the box and the accumulator
-                if (box.mode == 1) {
-                    stage_box<IT>(box, g, b0, b1, b2, a.in + ((long long)o.b * g.nc + c) * g.n0, buf);
-                    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
-                }
-                const float M = __uint_as_float(a.fmax[(long long)o.b * g.nc + c]);
-                float bound = 0.f;
-#pragma unroll
-                for (int q = 0; q < V; ++q) {
-                    const IT v = tv.template index<IT>(o, q);
-                    if (v >= 0 && (valid >> q & 1)) bound += 2.f * (M + fabsf(__ldg(gc + v)));
-                }
-#pragma unroll
-                for (int off = 16; off > 0; off >>= 1) bound += __shfl_xor_sync(0xffffffffu, bound, off);
-                if (lane == 0) sred[warp] = bound;
-                __syncthreads();   // the box of channel c and every warp's bound are in
-                float S = 0.f;
-                for (int w = 0; w < kThreads / 32; ++w) S += sred[w];
-                E = scale_exponent(S);
-            }
-            const bool fixed = E != INT_MIN && E != INT_MAX;
-            FixedScale fs;
-            fs.set(fixed ? E : 0);
-#pragma unroll
-            for (int q = 0; q < V; ++q) {
-                const IT v = tv.template index<IT>(o, q);
-                if (v < 0) continue;
-                const int lin = threadIdx.x + q * kThreads;
-                float x0, x1, x2;
-                if (!load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2)) {
-                    loss += (double)qnan();   // pull is NaN here, and so is the loss
-                    continue;
-                }
-                valid |= 1u << q;
-                const float gv = c == 0 ? slot[3 * NV + lin] : __ldg(gc + v);
-                float res, grad[3];
-                if (box.mode == 1) {
-                    W3<DP, 1> wx, wy, wz;
-                    const int ox = spline_taps32<DP, 1>(x0, wx.w, wx.dw, wx.hw) - box.xo;
-                    const int oy = spline_taps32<DP, 1>(x1, wy.w, wy.dw, wy.hw) - box.lo[1];
-                    const int oz = spline_taps32<DP, 1>(x2, wz.w, wz.dw, wz.hw) - box.lo[2];
-                    const unsigned P4 = 4u * box.P, Q4 = 4u * box.Q;
-                    const unsigned off = 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
-                    const unsigned p = smem_addr(buf) + off;
-                    float r[6];
-                    contract<kPullValGrad, DP>(wx, wy, wz, DP, DP, DP, false,
-                                               [&](int k, int jj, int i) { return lds_f32(p + k * Q4 + jj * P4 + 4u * i); },
-                                               r);
-                    res = r[3] - gv;
-                    grad[0] = r[0];
-                    grad[1] = r[1];
-                    grad[2] = r[2];
-                    const float d = 2.f * res;
-                    if (finitef(d) && E != INT_MAX) {
-                        if (fixed)
-                            push_scatter<DP, kPush, true>(wx, wy, wz, d * fs.inv_q1, 0.f, 0.f, acc_base + off, P4, Q4,
-                                                          lo_off);
-                        else
-                            push_scatter<DP, kPush, false>(wx, wy, wz, d, 0.f, 0.f, acc_base + off, P4, Q4, lo_off);
-                    }
-                } else {
-                    res = fused_voxel_global<DP, IT>(a, o.b, c, (long long)v, x0, x1, x2, gv, grad);
-                }
-                loss += (double)(res * res);
-                const float d = 2.f * res;
-                dphi[q][0] = fmaf(d, grad[0], dphi[q][0]);
-                dphi[q][1] = fmaf(d, grad[1], dphi[q][1]);
-                dphi[q][2] = fmaf(d, grad[2], dphi[q][2]);
-            }
-            __syncthreads();   // the scatter is complete
-            if (box.mode == 1 && E != INT_MAX) {
-                float* df = a.out + ((long long)o.b * g.nc + c) * g.n0;
-                if (fixed)
-                    flush_box<IT>(box, g, b0, b1, b2, df, [&](int si) {
-                        const float v = fixed_value(acc_hi[si], acc_lo[si], fs);
-                        acc_hi[si] = 0;
-                        acc_lo[si] = 0;
-                        return v;
-                    });
-                else
-                    flush_box<IT>(box, g, b0, b1, b2, df, [&](int si) {
-                        const float v = accf[si];
-                        accf[si] = 0.f;
-                        return v;
-                    });
-            }
-        }
-        // deformation cotangent of every sample voxel of the tile
-        float* dp = a.out2 + (long long)o.b * 3 * n1;
-#pragma unroll
-        for (int q = 0; q < V; ++q) {
-            const IT v = tv.template index<IT>(o, q);
-            if (v < 0) continue;
-            const bool ok = valid >> q & 1;
-            dp[v] = ok ? dphi[q][0] : qnan();
-            dp[v + n1] = ok ? dphi[q][1] : qnan();
-            dp[v + 2 * n1] = ok ? dphi[q][2] : qnan();
-        }
-        __syncthreads();   // ring slot j, the box buffer and the accumulator are free
-        if (j + kStages < ntl)
-            ring_fill<V, 1, TMA, IT>(ring, j + kStages, T0 + (j + kStages) * G, a, t, tv, phimap, gmap, a.up);
-        if (!TMA) __syncthreads();
-    }
-    // this CTA's loss partial
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
-    if (lane == 0) dred[warp] = loss;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double sum = 0.0;
-        for (int w = 0; w < kThreads / 32; ++w) sum += dred[w];
-        a.partial[blockIdx.x] = sum;
-    }
-}
-
-
-// ---- batched uneven workload ------------------------------------------------
-//
-// Tiles of all items form one queue; a CTA takes the next tile with an atomic
-// counter (dynamic load balance over volumes of uneven size and degree),
-// evaluates pull for the tile from its staged image box, writes f1, and pushes
-// the same values through the same box into the shared accumulator, which it
-// flushes into the item's output.  Shared memory is split into a fixed
-// accumulator region (two words per element) and the image box.
-
-template <int DP>
-__device__ __forceinline__ void batch_tile(const BatchItem& it, int lt, float* sm, int cap, Box& box,
-                                           int (&red)[8][7], float (&sred)[8]) {
-    constexpr int V = 2;
-    constexpr int NV = kThreads * V;
-    const LaunchArgs& a = it.pull;
-    const LaunchArgs& pb = it.push;
-    const Geometry& g = a.g;
-    const long long n1 = g.n1;
-    const TileGrid& t = it.t;
-    const ThreadVox<V> tv(t, g);
-    const TileOrigin o = tile_origin(t, lt);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int accw = ((2 * cap / 3) + 3) & ~3;   // accumulator words (fixed region)
-    float* accf = sm;
-    float* fbox = sm + accw;
-
-    float X[V][3];
-    int iv[V];
-    unsigned ok = 0;
-    int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
-#pragma unroll
-    for (int q = 0; q < V; ++q) {
-        iv[q] = tv.template index<int>(o, q);
-        if (iv[q] < 0) continue;
-        const float* phi = a.phi + iv[q];
-        if (!load_valid(__ldg(phi), __ldg(phi + n1), __ldg(phi + 2 * n1), g, X[q][0], X[q][1], X[q][2])) continue;
-        ok |= 1u << q;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const int f = first_tap32(X[q][k], DP);
-            const int cl = f < -kClamp ? -kClamp : (f > kClamp ? kClamp : f);
-            mn[k] = min(mn[k], cl);
-            mx[k] = max(mx[k], cl);
-        }
-    }
-    reduce_box<DP>(mn, mx, t, g, 3, box, red);   // 3 words per element: 2 accumulator + 1 image
-    if (box.mode != 1) {
-#pragma unroll
-        for (int q = 0; q < V; ++q) {
-            if (iv[q] < 0) continue;
-            if (!(ok >> q & 1)) {
-                pull_voxel_nan<kPull>(a, 0, iv[q]);
-                continue;
-            }
-            pull_tile_fallback<DP, kPull, int>(a, 0, iv[q], X[q][0], X[q][1], X[q][2]);
-            push_tile_fallback<DP, kPush, int>(pb, 0, iv[q], X[q][0], X[q][1], X[q][2]);
-        }
-        __syncthreads();   // box record reused by the next tile
-        return;
-    }
-    const unsigned acc_base = smem_addr(accf);
-    const unsigned lo_off = 4u * (unsigned)box.size;
-    int* acc_hi = reinterpret_cast<int*>(accf);
-    int* acc_lo = acc_hi + box.size;
-    for (int c = 0; c < g.nc; ++c) {
-        int b0, b1, b2;
-        bnd_code(a, c, b0, b1, b2);
-        stage_box<int>(box, g, b0, b1, b2, a.in + (long long)c * g.n0, fbox);
-        asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
-        __syncthreads();
-        float val[V];
-        float bound = 0.f;
-        float* f1 = a.out + (long long)c * n1;
-#pragma unroll
-        for (int q = 0; q < V; ++q) {
-            val[q] = 0.f;
-            if (iv[q] < 0) continue;
-            if (!(ok >> q & 1)) {
-                f1[iv[q]] = qnan();
-                continue;
-            }
-            W3<DP, 0> wx, wy, wz;
-            const int ox = spline_taps32<DP, 0>(X[q][0], wx.w, wx.dw, wx.hw) - box.xo;
-            const int oy = spline_taps32<DP, 0>(X[q][1], wy.w, wy.dw, wy.hw) - box.lo[1];
-            const int oz = spline_taps32<DP, 0>(X[q][2], wz.w, wz.dw, wz.hw) - box.lo[2];
-            const unsigned P4 = 4u * box.P, Q4 = 4u * box.Q;
-            const unsigned p = smem_addr(fbox) + 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
-            float r[6];
-            contract<kPull, DP>(wx, wy, wz, DP, DP, DP, false,
-                                [&](int k, int jj, int i) { return lds_f32(p + k * Q4 + jj * P4 + 4u * i); }, r);
-            f1[iv[q]] = r[0];
-            val[q] = r[0];
-            if (finitef(r[0])) bound += fabsf(r[0]);
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) bound += __shfl_xor_sync(0xffffffffu, bound, off);
-        if (lane == 0) sred[warp] = bound;
-        __syncthreads();   // bounds in; the image box is no longer read
-        float S = 0.f;
-        for (int w = 0; w < kThreads / 32; ++w) S += sred[w];
-        const int E = scale_exponent(S);
-        if (E != INT_MAX) {
-            const bool fixed = E != INT_MIN;
-            FixedScale fs;
-            fs.set(fixed ? E : 0);
-#pragma unroll
-            for (int q = 0; q < V; ++q) {
-                if (!(ok >> q & 1) || !finitef(val[q])) continue;
-                W3<DP, 0> wx, wy, wz;
-                const int ox = spline_taps32<DP, 0>(X[q][0], wx.w, wx.dw, wx.hw) - box.xo;
-                const int oy = spline_taps32<DP, 0>(X[q][1], wy.w, wy.dw, wy.hw) - box.lo[1];
-                const int oz = spline_taps32<DP, 0>(X[q][2], wz.w, wz.dw, wz.hw) - box.lo[2];
-                const unsigned P4 = 4u * box.P, Q4 = 4u * box.Q;
-                const unsigned base = acc_base + 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
-                if (fixed) push_scatter<DP, kPush, true>(wx, wy, wz, val[q] * fs.inv_q1, 0.f, 0.f, base, P4, Q4, lo_off);
-                else push_scatter<DP, kPush, false>(wx, wy, wz, val[q], 0.f, 0.f, base, P4, Q4, lo_off);
-            }
-            __syncthreads();   // the scatter is complete
-            float* out = pb.out + (long long)c * g.n0;
-            if (fixed)
-                flush_box<int>(box, g, b0, b1, b2, out, [&](int si) {
-                    const float v = fixed_value(acc_hi[si], acc_lo[si], fs);
-                    acc_hi[si] = 0;
-                    acc_lo[si] = 0;
-                    return v;
-                });
-            else
-                flush_box<int>(box, g, b0, b1, b2, out, [&](int si) {
-                    const float v = accf[si];
-                    accf[si] = 0.f;
-                    return v;
-                });
-        }
-        __syncthreads();   // accumulator clear, image box and sred reusable
-    }
-}
-
-__global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchItem* __restrict__ items, int nitems, int total,
-                                                       unsigned* counter, int cap) {
-    extern __shared__ __align__(128) float4 smem4[];
-    __shared__ int red[8][7];
-    __shared__ float sred[8];
-    __shared__ Box box;
-    __shared__ int s_tile;
-    float* sm = reinterpret_cast<float*>(smem4);
-    const int accw = ((2 * cap / 3) + 3) & ~3;
-    for (int i = threadIdx.x; i < (accw >> 2); i += kThreads)
-        reinterpret_cast<float4*>(sm)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
-        __syncthreads();
-        const int T = s_tile;
-        __syncthreads();   // every thread has read the tile before the next claim
-        if (T >= total) break;
-        int lo = 0, hi = nitems - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (items[mid].tile_begin <= T) lo = mid;
-            else hi = mid - 1;
-        }
-        const BatchItem& it = items[lo];
-        const int lt = T - it.tile_begin;
-        switch (it.dp) {
-            case 1: batch_tile<1>(it, lt, sm, cap, box, red, sred); break;
-            case 2: batch_tile<2>(it, lt, sm, cap, box, red, sred); break;
-            case 3: batch_tile<3>(it, lt, sm, cap, box, red, sred); break;
-            case 4: batch_tile<4>(it, lt, sm, cap, box, red, sred); break;
-            default: batch_tile<5>(it, lt, sm, cap, box, red, sred); break;
-        }
-    }
-}
-
-TileGrid make_grid(const LaunchArgs& a, const TileCfg& c) {
-    TileGrid t;
-    t.lx = c.lx;
-    t.ly = c.ly;
-    t.lz = c.lz;
-    t.ntx = (int)((a.g.d1[0] + (1 << c.lx) - 1) >> c.lx);
-    t.nty = (int)((a.g.d1[1] + (1 << c.ly) - 1) >> c.ly);
-    t.ntz = (int)((a.g.d1[2] + (1 << c.lz) - 1) >> c.lz);
-    t.cap = c.cap;
-    t.ntiles = t.ntx * t.nty * t.ntz * a.g.nb;
-    auto magic = [](int d, unsigned long long& m, int& sh) {
-        int l = 0;
-        while ((1LL << l) < d) ++l;                        // l = ceil(log2 d)
-        sh = 31 + l;
-        m = ((1ULL << sh) + (unsigned long long)d - 1) / (unsigned long long)d;
-    };
-    magic(t.ntx, t.mx, t.sx);
-    magic(t.nty, t.my, t.sy);
-    magic(t.ntz, t.mz, t.sz);
-    const int tx = 1 << c.lx;
-    t.pmod = tx >= 32 ? 0 : tx;
-    return t;
-}
-
-// Raise a kernel's dynamic shared-memory limit once per (device, kernel) to the
-// largest size requested so far.
-template <typename K>
-cudaError_t opt_in(K kern, size_t smem) {
-    static std::mutex mu;
-    static std::map<std::pair<int, const void*>, size_t> configured;
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    const auto key = std::make_pair(dev, reinterpret_cast<const void*>(kern));
-    std::lock_guard<std::mutex> lk(mu);
-    auto it = configured.find(key);
-    if (it != configured.end() && it->second >= smem) return cudaSuccess;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured[key] = smem;
-    return cudaSuccess;
-}
-
-// ---- TMA tensor maps (encoded on the host through the driver entry point) ----
-using EncodeFn = PFN_cuTensorMapEncodeTiled_v12000;
-
-EncodeFn encode_fn() {
-    static std::once_flag once;
-    static EncodeFn fn = nullptr;
-    std::call_once(once, [] {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeFn>(p);
-    });
-    return fn;
-}
-
-// 4-D map over a column-major volume stack (d0, d1, d2, planes) with a box of
-// one tile (TX, TY, TZ, comps).  Requires a 16-byte aligned base and d0 % 4 == 0.
-bool encode_tile_map(CUtensorMap* map, const float* base, const long long d[3], long long planes,
-                     const TileGrid& t, int comps) {
-    EncodeFn fn = encode_fn();
-    if (!fn) return false;
-    if ((reinterpret_cast<uintptr_t>(base) & 15) || (d[0] & 3) || (1 << t.lx) < 4) return false;
-    const cuuint64_t dims[4] = {(cuuint64_t)d[0], (cuuint64_t)d[1], (cuuint64_t)d[2], (cuuint64_t)planes};
-    for (int k = 0; k < 4; ++k)
-        if (dims[k] == 0 || dims[k] > (1ULL << 32)) return false;
-    const cuuint64_t strides[3] = {(cuuint64_t)d[0] * 4, (cuuint64_t)(d[0] * d[1]) * 4,
-                                   (cuuint64_t)(d[0] * d[1] * d[2]) * 4};
-    for (int k = 0; k < 3; ++k)
-        if (strides[k] >= (1ULL << 40)) return false;
-    const cuuint32_t box[4] = {(cuuint32_t)(1 << t.lx), (cuuint32_t)(1 << t.ly), (cuuint32_t)(1 << t.lz),
-                               (cuuint32_t)comps};
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
-    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dims, strides, box, estr,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS;
-}
-
-template <typename K, typename... Args>
-cudaError_t launch_persistent(K kern, const TileGrid& t, size_t smem, cudaStream_t s, const Args&... args) {
-    cudaError_t e = opt_in(kern, smem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    const long long want = (long long)sm_count() * per_sm;
-    const int grid = (int)(t.ntiles < want ? t.ntiles : want);
-    kern<<<grid, kThreads, smem, s>>>(args...);
-    return cudaGetLastError();
-}
-
-template <int DP, int OP, int V, typename IT, bool PUSH>
-cudaError_t launch_v(const LaunchArgs& a, const TileGrid& t, cudaStream_t s) {
-    constexpr int NV = kThreads * V;
-    CUtensorMap phimap, valmap;
-    std::memset(&phimap, 0, sizeof phimap);
-    std::memset(&valmap, 0, sizeof valmap);
-    const long long nb = a.g.nb, nc = a.g.nc;
-    bool tma = encode_tile_map(&phimap, a.phi, a.g.d1, 3 * nb, t, 3);
-    if constexpr (PUSH) {
-        constexpr int NCOMP = OP == kPushGrad ? 3 : 1;
-        tma = tma && encode_tile_map(&valmap, a.in, a.g.d1, NCOMP * nc * nb, t, NCOMP);
-        const size_t smem = (size_t)kStages * (3 + NCOMP) * NV * 4 + (size_t)t.cap * 4 + 8 * kStages;
-        if (tma) return launch_persistent(k_push_tiled<DP, OP, V, IT, true>, t, smem, s, a, t, phimap, valmap);
-        return launch_persistent(k_push_tiled<DP, OP, V, IT, false>, t, smem, s, a, t, phimap, valmap);
-    } else {
-        const size_t smem = (size_t)kStages * 3 * NV * 4 + 2 * (size_t)t.cap * 4 + 8 * kStages;
-        if (tma) return launch_persistent(k_pull_tiled<DP, OP, V, IT, true>, t, smem, s, a, t, phimap);
-        return launch_persistent(k_pull_tiled<DP, OP, V, IT, false>, t, smem, s, a, t, phimap);
-    }
-}
-
-template <int DP, int V, typename IT>
-cudaError_t launch_fused_v(const LaunchArgs& a, const TileGrid& t, cudaStream_t s, int grid) {
-    constexpr int NV = kThreads * V;
-    CUtensorMap phimap, gmap;
-    std::memset(&phimap, 0, sizeof phimap);
-    std::memset(&gmap, 0, sizeof gmap);
-    const long long nb = a.g.nb, nc = a.g.nc;
-    const bool tma = encode_tile_map(&phimap, a.phi, a.g.d1, 3 * nb, t, 3) &&
-                     encode_tile_map(&gmap, a.up, a.g.d1, nc * nb, t, 1);
-    const size_t smem = (size_t)kStages * 4 * NV * 4 + 4 * (size_t)t.cap * 4 + 8 * kStages;
-    cudaError_t e;
-    if (tma) {
-        auto k = k_fused_tiled<DP, V, IT, true>;
-        if ((e = opt_in(k, smem)) != cudaSuccess) return e;
-        k<<<grid, kThreads, smem, s>>>(a, t, phimap, gmap);
-    } else {
-        auto k = k_fused_tiled<DP, V, IT, false>;
-        if ((e = opt_in(k, smem)) != cudaSuccess) return e;
-        k<<<grid, kThreads, smem, s>>>(a, t, phimap, gmap);
-    }
-    return cudaGetLastError();
-}
-
-template <int DP, typename IT>
-cudaError_t launch_fused_dp(const LaunchArgs& a, const TileCfg& c, cudaStream_t s, int grid) {
-    const TileGrid t = make_grid(a, c);
-    if ((1 << (c.lx + c.ly + c.lz)) > kThreads) return launch_fused_v<DP, 2, IT>(a, t, s, grid);
-    return launch_fused_v<DP, 1, IT>(a, t, s, grid);
-}
-
-template <int DP, int OP, typename IT, bool PUSH>
-cudaError_t launch_one(const LaunchArgs& a, const TileCfg& c, cudaStream_t s) {
-    const TileGrid t = make_grid(a, c);
-    const int vox = 1 << (c.lx + c.ly + c.lz);
-    if (vox > kThreads) return launch_v<DP, OP, 2, IT, PUSH>(a, t, s);
-    return launch_v<DP, OP, 1, IT, PUSH>(a, t, s);
-}
-
-template <int OP, typename IT, bool PUSH>
-cudaError_t dispatch(const LaunchArgs& a, const TileCfg& t, cudaStream_t s) {
-    switch (a.g.dp[0]) {
-        case 1: return launch_one<1, OP, IT, PUSH>(a, t, s);
-        case 2: return launch_one<2, OP, IT, PUSH>(a, t, s);
-        case 3: return launch_one<3, OP, IT, PUSH>(a, t, s);
-        case 4: return launch_one<4, OP, IT, PUSH>(a, t, s);
-        default: return launch_one<5, OP, IT, PUSH>(a, t, s);
-    }
-}
-
-}  // namespace
+cudaError_t launch_tiled_pull_basic(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s);
+cudaError_t launch_tiled_pull_hess(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s);
+cudaError_t launch_tiled_pull_dot(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s);
+cudaError_t launch_tiled_push(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s);
+cudaError_t launch_tiled_push_grad(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s);
+unsigned status_pull_basic(bool reset);
+unsigned status_pull_hess(bool reset);
+unsigned status_pull_dot(bool reset);
+unsigned status_push(bool reset);
+unsigned status_push_grad(bool reset);
+unsigned status_fused(bool reset);
+unsigned status_batch(bool reset);
 
 bool tiled_supported(const LaunchArgs& a, const TileCfg& t) {
     const Geometry& g = a.g;
@@ -1500,26 +37,16 @@ bool tiled_supported(const LaunchArgs& a, const TileCfg& t) {
 }
 
 cudaError_t launch_pull_tiled(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s) {
-    const bool small = a.g.n0 < (1LL << 31) - 1 && a.g.n1 < (1LL << 31) - 1;
     switch (op) {
-        case kPull: return small ? dispatch<kPull, int, false>(a, t, s) : dispatch<kPull, long long, false>(a, t, s);
-        case kPullGrad:
-            return small ? dispatch<kPullGrad, int, false>(a, t, s) : dispatch<kPullGrad, long long, false>(a, t, s);
-        case kPullHess:
-            return small ? dispatch<kPullHess, int, false>(a, t, s) : dispatch<kPullHess, long long, false>(a, t, s);
-        case kPullGradDot:
-            return small ? dispatch<kPullGradDot, int, false>(a, t, s)
-                         : dispatch<kPullGradDot, long long, false>(a, t, s);
-        default:
-            return small ? dispatch<kPullHessDot, int, false>(a, t, s)
-                         : dispatch<kPullHessDot, long long, false>(a, t, s);
+        case kPull:
+        case kPullGrad: return launch_tiled_pull_basic(op, a, t, s);
+        case kPullHess: return launch_tiled_pull_hess(op, a, t, s);
+        default: return launch_tiled_pull_dot(op, a, t, s);
     }
 }
 
 cudaError_t launch_push_tiled(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s) {
-    const bool small = a.g.n0 < (1LL << 31) - 1 && a.g.n1 < (1LL << 31) - 1;
-    if (op == kPush) return small ? dispatch<kPush, int, true>(a, t, s) : dispatch<kPush, long long, true>(a, t, s);
-    return small ? dispatch<kPushGrad, int, true>(a, t, s) : dispatch<kPushGrad, long long, true>(a, t, s);
+    return op == kPush ? launch_tiled_push(op, a, t, s) : launch_tiled_push_grad(op, a, t, s);
 }
 
 int fused_tiled_grid(const LaunchArgs& a, const TileCfg& c) {
@@ -1529,42 +56,16 @@ int fused_tiled_grid(const LaunchArgs& a, const TileCfg& c) {
     return (int)(t.ntiles < want ? t.ntiles : want);
 }
 
-cudaError_t launch_fused_tiled(const LaunchArgs& a, const TileCfg& t, cudaStream_t s, int grid) {
-    const bool small = a.g.n0 < (1LL << 31) - 1 && a.g.n1 < (1LL << 31) - 1;
-    switch (a.g.dp[0]) {
-        case 1: return small ? launch_fused_dp<1, int>(a, t, s, grid) : launch_fused_dp<1, long long>(a, t, s, grid);
-        case 2: return small ? launch_fused_dp<2, int>(a, t, s, grid) : launch_fused_dp<2, long long>(a, t, s, grid);
-        case 3: return small ? launch_fused_dp<3, int>(a, t, s, grid) : launch_fused_dp<3, long long>(a, t, s, grid);
-        case 4: return small ? launch_fused_dp<4, int>(a, t, s, grid) : launch_fused_dp<4, long long>(a, t, s, grid);
-        default: return small ? launch_fused_dp<5, int>(a, t, s, grid) : launch_fused_dp<5, long long>(a, t, s, grid);
-    }
-}
-
 TileGrid tile_grid(const LaunchArgs& a, const TileCfg& c) { return make_grid(a, c); }
 
-cudaError_t launch_batch(const BatchItem* items, int nitems, int total_tiles, unsigned* counter, int cap,
-                         cudaStream_t s) {
-    const size_t smem = (size_t)cap * sizeof(float);
-    cudaError_t e = opt_in(k_batch, smem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kThreads, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    const long long want = (long long)sm_count() * per_sm;
-    const int grid = (int)(total_tiles < want ? total_tiles : want);
-    if (grid < 1) return cudaSuccess;
-    k_batch<<<grid, kThreads, smem, s>>>(items, nitems, total_tiles, counter, cap);
-    return cudaGetLastError();
-}
-
 unsigned read_device_status(bool reset) {
-    unsigned v = 0;
-    if (cudaMemcpyFromSymbol(&v, g_device_status, sizeof v) != cudaSuccess) return 0xffffffffu;
-    if (reset) {
-        const unsigned z = 0;
-        cudaMemcpyToSymbol(g_device_status, &z, sizeof z);
-    }
+    unsigned v = status_pull_basic(reset);
+    v |= status_pull_hess(reset);
+    v |= status_pull_dot(reset);
+    v |= status_push(reset);
+    v |= status_push_grad(reset);
+    v |= status_fused(reset);
+    v |= status_batch(reset);
     return v;
 }
 
