@@ -26,6 +26,7 @@ struct TileGrid {
     int sx, sy, sz;
     int cap;            // box budget in floats
     int pmod;           // box row pitch P is chosen with P % 32 == pmod
+    int img_tma;        // pull: interior boxes may be loaded with one TMA copy (image tensor map valid)
 };
 
 // Fused forward + adjoint step over tiles: grid size for a launch, and the

@@ -69,6 +69,10 @@ constexpr int kThreads = 256;
 constexpr int kStages = 4;                 // tiles of the ring in flight per CTA
 constexpr unsigned kStatusWaitTimeout = 1u;
 constexpr int kClamp = 1 << 29;    // first taps are clamped to +-kClamp for the box reduction
+// Fixed image window for TMA-staged pull boxes: row pitch 24 (24 % 32 places
+// the 4 rows of an 8-wide warp tile in disjoint bank ranges), 16 rows, 16 planes.
+constexpr int kTmaBoxX = 24, kTmaBoxY = 16, kTmaBoxZ = 16;
+constexpr int kTmaBoxFloats = kTmaBoxX * kTmaBoxY * kTmaBoxZ;
 
 template <int DP, int ORD>
 struct W3 {
@@ -131,6 +135,7 @@ struct Box {
     int P, Q, size; // row pitch (P % 32 == pmod, P % 4 == 0), plane pitch (multiple of 32), floats
     int mode;       // 0 no valid voxel, 1 shared memory, 2 per-voxel global fallback
     int interior;   // bit k: the box lies inside the image along dimension k (no folding)
+    int tma;        // 1: the box is the fixed kTmaBox* window loaded by one TMA copy
     float S;        // block sum of the caller's per-thread value (push: bound on sum |contribution|)
     int E;          // scale exponent of the fixed-point accumulator for S (see scale_exponent)
 };
@@ -193,6 +198,7 @@ __device__ __forceinline__ void reduce_box(int (&mn)[3], int (&mx)[3], const Til
             }
         if (lo[0] > hi[0]) {
             box.mode = 0;
+            box.tma = 0;
         } else {
             const int xo = lo[0] & ~3;
             long long e[3];
@@ -213,18 +219,28 @@ __device__ __forceinline__ void reduce_box(int (&mn)[3], int (&mx)[3], const Til
             } else {
                 Q = (P * e[1] + 3) & ~3LL;
             }
-            const long long size = Q * e[2];
+            long long size = Q * e[2];
             const bool fits = e[0] <= 4096 && e[1] <= 4096 && e[2] <= 4096 && size * words <= t.cap;
             box.mode = fits ? 1 : 2;
+            box.tma = 0;
+            if (words == 1 && t.img_tma && interior == 7 && e[0] <= kTmaBoxX && e[1] <= kTmaBoxY &&
+                e[2] <= kTmaBoxZ) {
+                box.mode = 1;
+                box.tma = 1;
+                P = kTmaBoxX;
+                Q = kTmaBoxX * kTmaBoxY;
+                size = kTmaBoxFloats;
+            }
+            const bool staged = box.mode == 1;
             box.lo[0] = lo[0];
             box.lo[1] = lo[1];
             box.lo[2] = lo[2];
             box.xo = xo;
 #pragma unroll
-            for (int k = 0; k < 3; ++k) box.ext[k] = fits ? (int)e[k] : 0;
-            box.P = fits ? (int)P : 0;
-            box.Q = fits ? (int)Q : 0;
-            box.size = fits ? (int)size : 0;
+            for (int k = 0; k < 3; ++k) box.ext[k] = staged ? (int)e[k] : 0;
+            box.P = staged ? (int)P : 0;
+            box.Q = staged ? (int)Q : 0;
+            box.size = staged ? (int)size : 0;
             box.interior = interior;
         }
     }
@@ -797,7 +813,8 @@ __device__ __forceinline__ void pull_compute(const LaunchArgs& a, const TileOrig
 template <int DP, int OP, int V, typename IT, bool TMA>
 __global__ void __launch_bounds__(kThreads, 2) k_pull_tiled(const __grid_constant__ LaunchArgs a,
                                                             const __grid_constant__ TileGrid t,
-                                                            const __grid_constant__ CUtensorMap phimap) {
+                                                            const __grid_constant__ CUtensorMap phimap,
+                                                            const __grid_constant__ CUtensorMap imgmap) {
     extern __shared__ __align__(128) float4 smem4[];
     constexpr int NV = kThreads * V;
     __shared__ int red[8][7];
@@ -816,17 +833,36 @@ __global__ void __launch_bounds__(kThreads, 2) k_pull_tiled(const __grid_constan
     ring.slot_floats = 3 * NV;
     float* bufs = sm + kStages * 3 * NV;
     ring.bars = smem_addr(bufs + 2 * t.cap);
+    const unsigned bbar = ring.bars + 8u * kStages;   // one mbarrier per box buffer (TMA-staged boxes)
+    unsigned bphase = 0;                              // bit b: parity of buffer b's next TMA completion
     if (threadIdx.x == 0) {
         s_abort = 0;
         if (TMA) {
             for (int k = 0; k < kStages; ++k) mbar_init(ring.bars + 8u * k, 1);
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
+        mbar_init(bbar, 1);
+        mbar_init(bbar + 8u, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     for (int j = 0; j < kStages && j < ntl; ++j)
         ring_fill<V, 0, TMA, IT>(ring, j, T0 + j * G, a, t, tv, phimap, phimap, a.in);
     if (!TMA) __syncthreads();
+
+    // one TMA copy of channel c's fixed image window into buffer `buf` (thread 0)
+    auto tma_box = [&](const Box& box, int b, int c, int buf) {
+        if (threadIdx.x == 0) {
+            const unsigned bar = bbar + 8u * buf;
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(bar, (unsigned)(kTmaBoxFloats * sizeof(float)));
+            tma_load_4d(smem_addr(bufs + buf * t.cap), &imgmap, bar, box.xo, box.lo[1], box.lo[2], b * g.nc + c);
+        }
+    };
+    // every thread: wait for buffer buf's TMA copy
+    auto tma_wait = [&](int buf) {
+        if (!mbar_wait(bbar + 8u * buf, (bphase >> buf) & 1u)) s_abort = 1;
+        bphase ^= 1u << buf;
+    };
 
     // box of tile j (its deformation must be in the ring), staged into buffer j & 1
     auto prepare = [&](int j) {
@@ -837,9 +873,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_pull_tiled(const __grid_constan
         tile_bounds<DP, V, IT>(g, o, tv, slot, mn, mx);
         reduce_box<DP>(mn, mx, t, g, 1, boxm[j & 1], red);
         if (boxm[j & 1].mode == 1) {
-            int b0, b1, b2;
-            bnd_code(a, 0, b0, b1, b2);
-            stage_box<IT>(boxm[j & 1], g, b0, b1, b2, a.in + (long long)o.b * g.nc * g.n0, bufs + (j & 1) * t.cap);
+            if (boxm[j & 1].tma) {
+                tma_box(boxm[j & 1], o.b, 0, j & 1);
+            } else {
+                int b0, b1, b2;
+                bnd_code(a, 0, b0, b1, b2);
+                stage_box<IT>(boxm[j & 1], g, b0, b1, b2, a.in + (long long)o.b * g.nc * g.n0,
+                              bufs + (j & 1) * t.cap);
+            }
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     };
@@ -852,6 +893,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pull_tiled(const __grid_constan
         } else {
             asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         }
+        if (boxm[j & 1].tma) tma_wait(j & 1);   // the record was published by prepare(j)'s barrier
         __syncthreads();   // box j is in its buffer
         if (s_abort) break;
         const TileOrigin o = tile_origin(t, T0 + j * G);
@@ -873,14 +915,21 @@ __global__ void __launch_bounds__(kThreads, 2) k_pull_tiled(const __grid_constan
         for (int c = 1; c < g.nc; ++c) {
             __syncthreads();   // channel c-1 reads of the buffer are done
             if (box.mode == 1) {
-                int b0, b1, b2;
-                bnd_code(a, c, b0, b1, b2);
-                stage_box<IT>(box, g, b0, b1, b2, a.in + ((long long)o.b * g.nc + c) * g.n0, buf);
-                asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+                if (box.tma) {
+                    tma_box(box, o.b, c, j & 1);
+                    tma_wait(j & 1);
+                } else {
+                    int b0, b1, b2;
+                    bnd_code(a, c, b0, b1, b2);
+                    stage_box<IT>(box, g, b0, b1, b2, a.in + ((long long)o.b * g.nc + c) * g.n0, buf);
+                    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+                }
             }
             __syncthreads();
+            if (s_abort) break;
             pull_compute<DP, OP, V, IT>(a, o, tv, t, slot, c, box, buf, acc);
         }
+        if (s_abort) break;
         __syncthreads();   // ring slot j and buffer j & 1 are free
         if (j + kStages < ntl)
             ring_fill<V, 0, TMA, IT>(ring, j + kStages, T0 + (j + kStages) * G, a, t, tv, phimap, phimap, a.in);
@@ -909,8 +958,27 @@ __device__ __forceinline__ void push_scatter(const WT& wx, const WT& wy, const W
             const unsigned row = base + k * Q4 + j * P4;
             if constexpr (FIXED) {
                 int h[DP], l[DP];
+                // taps in pairs with the packed f32x2 pipe (each lane rounds exactly
+                // like the scalar sequence of the odd tap below)
 #pragma unroll
-                for (int i = 0; i < DP; ++i) {
+                for (int i = 0; i + 1 < DP; i += 2) {
+                    float2 y2;
+                    if constexpr (OP == kPushGrad)
+                        y2 = __ffma2_rn(make_float2(ca, ca), make_float2(wx.dw[i], wx.dw[i + 1]),
+                                        __fmul2_rn(make_float2(cb, cb), make_float2(wx.w[i], wx.w[i + 1])));
+                    else
+                        y2 = __fmul2_rn(make_float2(cb, cb), make_float2(wx.w[i], wx.w[i + 1]));
+                    const float2 t1 = __fadd2_rn(y2, make_float2(kMagic, kMagic));
+                    const float2 u = __fadd2_rn(t1, make_float2(-kMagic, -kMagic));
+                    const float2 r = __ffma2_rn(u, make_float2(-1.f, -1.f), y2);
+                    const float2 l2 = __ffma2_rn(r, make_float2(2097152.0f, 2097152.0f), make_float2(kMagic, kMagic));
+                    h[i] = __float_as_int(t1.x) - kMagicBits;
+                    h[i + 1] = __float_as_int(t1.y) - kMagicBits;
+                    l[i] = __float_as_int(l2.x) - kMagicBits;
+                    l[i + 1] = __float_as_int(l2.y) - kMagicBits;
+                }
+                if constexpr (DP & 1) {
+                    constexpr int i = DP - 1;
                     float y;
                     if constexpr (OP == kPushGrad) y = fmaf(ca, wx.dw[i], cb * wx.w[i]);
                     else y = cb * wx.w[i];
@@ -1586,6 +1654,7 @@ TileGrid make_grid(const LaunchArgs& a, const TileCfg& c) {
     magic(t.ntz, t.mz, t.sz);
     const int tx = 1 << c.lx;
     t.pmod = tx >= 32 ? 0 : tx;
+    t.img_tma = 0;
     return t;
 }
 
@@ -1648,6 +1717,28 @@ bool encode_tile_map(CUtensorMap* map, const float* base, const long long d[3], 
     return r == CUDA_SUCCESS;
 }
 
+// Tensor map of an image (d0[0], d0[1], d0[2], planes) with the fixed
+// kTmaBox* window as its box; false when TMA cannot address it (base or row
+// stride not 16-byte aligned, dimensions out of range).
+bool encode_box_map(CUtensorMap* map, const float* base, const long long d[3], long long planes) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    if ((reinterpret_cast<uintptr_t>(base) & 15) || (d[0] & 3)) return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)d[0], (cuuint64_t)d[1], (cuuint64_t)d[2], (cuuint64_t)planes};
+    for (int k = 0; k < 4; ++k)
+        if (dims[k] == 0 || dims[k] > (1ULL << 32)) return false;
+    const cuuint64_t strides[3] = {(cuuint64_t)d[0] * 4, (cuuint64_t)(d[0] * d[1]) * 4,
+                                   (cuuint64_t)(d[0] * d[1] * d[2]) * 4};
+    for (int k = 0; k < 3; ++k)
+        if (strides[k] >= (1ULL << 40)) return false;
+    const cuuint32_t box[4] = {(cuuint32_t)kTmaBoxX, (cuuint32_t)kTmaBoxY, (cuuint32_t)kTmaBoxZ, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 template <typename K, typename... Args>
 cudaError_t launch_persistent(K kern, const TileGrid& t, size_t smem, cudaStream_t s, const Args&... args) {
     cudaError_t e = opt_in(kern, smem);
@@ -1677,9 +1768,16 @@ cudaError_t launch_v(const LaunchArgs& a, const TileGrid& t, cudaStream_t s) {
         if (tma) return launch_persistent(k_push_tiled<DP, OP, V, IT, true>, t, smem, s, a, t, phimap, valmap);
         return launch_persistent(k_push_tiled<DP, OP, V, IT, false>, t, smem, s, a, t, phimap, valmap);
     } else {
-        const size_t smem = (size_t)kStages * 3 * NV * 4 + 2 * (size_t)t.cap * 4 + 8 * kStages;
-        if (tma) return launch_persistent(k_pull_tiled<DP, OP, V, IT, true>, t, smem, s, a, t, phimap);
-        return launch_persistent(k_pull_tiled<DP, OP, V, IT, false>, t, smem, s, a, t, phimap);
+        // interior boxes as one TMA copy of a fixed window when the tile is 8 wide
+        // (the window's row pitch is bank-conflict free for 8-wide warp tiles)
+        CUtensorMap imgmap;
+        std::memset(&imgmap, 0, sizeof imgmap);
+        TileGrid tt = t;
+        tt.img_tma = t.lx == 3 && t.cap >= kTmaBoxFloats && (t.cap & 31) == 0 &&
+                     encode_box_map(&imgmap, a.in, a.g.d0, nc * nb);
+        const size_t smem = (size_t)kStages * 3 * NV * 4 + 2 * (size_t)t.cap * 4 + 8 * kStages + 16;
+        if (tma) return launch_persistent(k_pull_tiled<DP, OP, V, IT, true>, tt, smem, s, a, tt, phimap, imgmap);
+        return launch_persistent(k_pull_tiled<DP, OP, V, IT, false>, tt, smem, s, a, tt, phimap, imgmap);
     }
 }
 
