@@ -150,6 +150,22 @@ int pp_fused_step_noalloc(double *loss, float *df, float *dphi, const float *f0,
                           const float *g, const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
                           const int *bnd, int nbnd, const int deg[3], int ext, int accumulate, void *stream);
 
+/* ---- affine resampling --------------------------------------------------- */
+/* Pull / push through the affine map x = Aff * (i, j, k, 1) of sample voxel
+ * (i, j, k) instead of a stored deformation.  Aff: HOST pointer to 12 floats,
+ * the 3x4 column-major matrix already adjusted to 0-based indices (the
+ * reference's adjust_affine, src/pushpull_cpu.jl:357-362); it is passed to the
+ * kernel by value.  Positions are rounded exactly as the reference CPU code
+ * (xj = Aff[3]*j + Aff[6]*k + Aff[9], then x = xj + Aff[0]*i).  Validity, NaN
+ * and skipping rules as pp_pull / pp_push.  Replaces affine_pull_element /
+ * affine_push_element (artifacts/C/pushpull.cu:187-231) and the per-slice
+ * ccall loops of src/pushpull_cpu.jl:268-349. */
+int pp_pull_affine(float *f1, const float *f0, const float *Aff, const pp_usize d0[3], const pp_usize d1[3],
+                   int nc, int nb, const int *bnd, int nbnd, const int deg[3], int ext, void *stream);
+int pp_push_affine(float *f0, const float *f1, const float *Aff, const pp_usize d0[3], const pp_usize d1[3],
+                   int nc, int nb, const int *bnd, int nbnd, const int deg[3], int ext, int accumulate,
+                   void *stream);
+
 /* ---- batched uneven workload ------------------------------------------- */
 /* One (image, deformation) pair of a batch: f1 = pull(f0, phi) is written and
  * out (+)= push(f1, phi) is accumulated, all device pointers, single batch,
@@ -239,6 +255,13 @@ void push (float *f0, const float *phi, const float *f1,
            const pp_usize *d0, const pp_usize n1, const int *bnd, const pp_usize *dp, const int ext);
 void pushg(float *g0, const float *phi, const float *g1,
            const pp_usize *d0, const pp_usize n1, const int *bnd, const pp_usize *dp, const int ext);
+/* artifacts/C/pushpull.h:11-14 (pushpull.c:176-243): Aff is the 3x4 column-major
+ * matrix already adjusted to 0-based indices (src/pushpull_cpu.jl:357-362);
+ * d1 = sample grid, n1 = d1[0]*d1[1]*d1[2]. */
+void pull_affine(float *f1, const float *f0, const pp_usize *d0, const pp_usize n1,
+                 const pp_usize *d1, const float *Aff, const int *bnd, const pp_usize *dp, const int ext);
+void push_affine(float *f0, const float *f1, const pp_usize *d0, const pp_usize n1,
+                 const pp_usize *d1, const float *Aff, const int *bnd, const pp_usize *dp, const int ext);
 
 #ifdef __cplusplus
 }

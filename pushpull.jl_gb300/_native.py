@@ -51,6 +51,10 @@ _SIGS = {
                                 _i32x3, C.c_int, C.c_int, _vp]),
     "pp_fused_step_noalloc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp,
                                         C.c_int, _i32x3, C.c_int, C.c_int, _vp]),
+    "pp_pull_affine": (C.c_int, [_vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int, _i32x3, C.c_int,
+                                 _vp]),
+    "pp_push_affine": (C.c_int, [_vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int, _i32x3, C.c_int,
+                                 C.c_int, _vp]),
     "pp_batch_create": (C.c_int, [C.POINTER(_vp), C.POINTER(BatchItem), C.c_int, C.c_int]),
     "pp_batch_tiles": (C.c_int, [_vp]),
     "pp_batch_run": (C.c_int, [_vp, _vp]),

@@ -9,6 +9,8 @@ stream.  There is no CPU path: CPU tensors are rejected.
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import torch
 
 from . import _native
@@ -125,6 +127,61 @@ def push_grad(g1: torch.Tensor, phi: torch.Tensor, d0, sett: Settings = Settings
               accumulate: bool = False) -> torch.Tensor:
     """Adjoint of ``pull_grad``: ``∇f (d₁…, 3, [C, [B]])`` -> ``(d₀…, [C, [B]])``."""
     return _push_family("pp_push_grad", g1, phi, d0, sett, True, out, accumulate)
+
+
+def adjust_affine(Aff) -> list:
+    """1-based 3x4 (or 4x4) affine -> 0-based 3x4, column-major as 12 floats
+    (src/pushpull_cpu.jl:357-362: the last column becomes the row sums minus 1,
+    computed in Float32)."""
+    A = torch.as_tensor(Aff, dtype=torch.float32).cpu()
+    assert A.dim() == 2 and A.shape[1] == 4 and A.shape[0] in (3, 4)
+    A = A[:3].clone()
+    A[:, 3] = A.sum(dim=1) - 1.0
+    return [float(v) for v in A.t().reshape(-1)]
+
+
+def _affine_family(push: bool, x, Aff, d_other, sett: Settings, out=None, accumulate=False):
+    assert 3 <= x.dim() <= 5, "input must have between 3 & 5 dimensions"
+    assert len(sett.bnd) == L.jsize(x, 4) or len(sett.bnd) == 1
+    _require_cuda(x)
+    x = L.colmajor(x)
+    nc, nb = L.jsize(x, 4), L.jsize(x, 5)
+    d_other = tuple(int(v) for v in d_other)
+    assert len(d_other) == 3
+    d_in = tuple(x.shape[:3])
+    d0, d1 = (d_other, d_in) if push else (d_in, d_other)
+    shape = d_other + tuple(x.shape[3:])
+    if out is None:
+        out = L.empty(shape, device=x.device)
+        accumulate = False
+    else:
+        _require_cuda(out)
+        assert tuple(out.shape) == shape and L.is_colmajor(out)
+    A = (C.c_float * 12)(*adjust_affine(Aff))
+    lib = _native.lib()
+    if push:
+        rc = lib.pp_push_affine(out.data_ptr(), x.data_ptr(), A, _native.u64x3(d0), _native.u64x3(d1), nc, nb,
+                                sett.bnd_array(), sett.nbnd, _native.i32x3(sett.deg), sett.ext,
+                                int(bool(accumulate)), _stream(x))
+        _native.check("pp_push_affine", rc)
+    else:
+        rc = lib.pp_pull_affine(out.data_ptr(), x.data_ptr(), A, _native.u64x3(d0), _native.u64x3(d1), nc, nb,
+                                sett.bnd_array(), sett.nbnd, _native.i32x3(sett.deg), sett.ext, _stream(x))
+        _native.check("pp_pull_affine", rc)
+    return out
+
+
+def affine_pull(f0: torch.Tensor, Aff, d1, sett: Settings = Settings(), *, out=None) -> torch.Tensor:
+    """Sample ``f₀`` on a ``d₁`` grid mapped by the 1-based affine ``Aff`` (3x4 or
+    4x4): ``f₁[i] = f₀(Aff * i)`` (src/pushpull_cpu.jl:268-307)."""
+    return _affine_family(False, f0, Aff, d1, sett, out)
+
+
+def affine_push(f1: torch.Tensor, Aff, d0, sett: Settings = Settings(), *, out=None,
+                accumulate: bool = False) -> torch.Tensor:
+    """Adjoint of ``affine_pull``: scatter ``f₁`` into a ``d₀`` grid
+    (src/pushpull_cpu.jl:310-349)."""
+    return _affine_family(True, f1, Aff, d0, sett, out, accumulate)
 
 
 def id(v: torch.Tensor = None, *, affine=None, dim=None, device=None) -> torch.Tensor:  # noqa: A001

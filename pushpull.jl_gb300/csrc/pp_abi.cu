@@ -557,6 +557,44 @@ int compat_call(int kind, float* out, const float* phi, const float* in, const p
     return PP_OK;
 }
 
+// pull_affine / push_affine on host pointers: one (channel, batch) slice, Aff
+// already 0-based (artifacts/C/pushpull.c:176-243)
+int compat_affine(bool push, float* out, const float* in, const pp_usize* d0, pp_usize n1, const pp_usize* d1,
+                  const float* Aff, const int* bnd, const pp_usize* dp, int ext) {
+    if (!d0 || !d1 || !bnd || !dp || !Aff) return pp::fail(PP_ERR_NULL, "d0, d1, Aff, bnd and dp must not be NULL");
+    int deg[3], b[3];
+    for (int k = 0; k < 3; ++k) {
+        if (dp[k] < 1 || dp[k] > 5) return pp::fail(PP_ERR_DEGREE, "dp[%d] = %llu outside 1..5", k, dp[k]);
+        deg[k] = (int)dp[k] - 1;
+        b[k] = (bnd[k] >= 0 && bnd[k] <= 2) ? bnd[k] : 1;
+    }
+    if (n1 != d1[0] * d1[1] * d1[2]) return pp::fail(PP_ERR_DIMS, "n1 must equal d1[0]*d1[1]*d1[2]");
+    if (n1 == 0) return PP_OK;
+    const pp_usize n0 = d0[0] * d0[1] * d0[2];
+    const size_t in_b = (push ? (size_t)n1 : (size_t)n0) * sizeof(float);
+    const size_t out_b = (push ? (size_t)n0 : (size_t)n1) * sizeof(float);
+    int rc = g_ws.reserve(round256(in_b) + round256(out_b));
+    if (rc != PP_OK) return rc;
+    float* din = (float*)g_ws.buf;
+    float* dout = (float*)((char*)g_ws.buf + round256(in_b));
+    cudaStream_t s = g_ws.stream;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(din, in, in_b, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return pp::cuda_fail(e, "copy input");
+    if (push && (e = cudaMemcpyAsync(dout, out, out_b, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return pp::cuda_fail(e, "copy accumulator");
+    rc = push ? pp_push_affine(dout, din, Aff, d0, d1, 1, 1, b, 1, deg, ext, 1, s)
+              : pp_pull_affine(dout, din, Aff, d0, d1, 1, 1, b, 1, deg, ext, s);
+    if (rc != PP_OK) {
+        cudaStreamSynchronize(s);
+        return rc;
+    }
+    if ((e = cudaMemcpyAsync(out, dout, out_b, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return pp::cuda_fail(e, "copy result");
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return pp::cuda_fail(e, "synchronize");
+    return PP_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -584,6 +622,16 @@ void push(float* f0, const float* phi, const float* f1, const pp_usize* d0, cons
 void pushg(float* g0, const float* phi, const float* g1, const pp_usize* d0, const pp_usize n1, const int* bnd,
            const pp_usize* dp, const int ext) {
     report("pushg", compat_call(4, g0, phi, g1, d0, n1, bnd, dp, ext));
+}
+
+void pull_affine(float* f1, const float* f0, const pp_usize* d0, const pp_usize n1, const pp_usize* d1,
+                 const float* Aff, const int* bnd, const pp_usize* dp, const int ext) {
+    report("pull_affine", compat_affine(false, f1, f0, d0, n1, d1, Aff, bnd, dp, ext));
+}
+
+void push_affine(float* f0, const float* f1, const pp_usize* d0, const pp_usize n1, const pp_usize* d1,
+                 const float* Aff, const int* bnd, const pp_usize* dp, const int ext) {
+    report("push_affine", compat_affine(true, f0, f1, d0, n1, d1, Aff, bnd, dp, ext));
 }
 
 }  // extern "C"

@@ -76,6 +76,19 @@ def reshape(t: torch.Tensor, shape) -> torch.Tensor:
     return flat.reshape(shape[::-1]).permute(*_rev(len(shape)))
 
 
+def flat(t: torch.Tensor) -> torch.Tensor:
+    """The elements of a column-major tensor in column-major order, as a 1-D view
+    (a copy only if ``t`` is not column-major)."""
+    t = colmajor(t)
+    return t.permute(*_rev(t.dim())).reshape(-1)
+
+
+def unflat(v: torch.Tensor, shape) -> torch.Tensor:
+    """Inverse of ``flat``: a 1-D tensor viewed as a column-major tensor of ``shape``."""
+    shape = tuple(int(s) for s in shape)
+    return v.reshape(shape[::-1]).permute(*_rev(len(shape)))
+
+
 def jsize(t, k: int) -> int:
     """Julia ``size(t, k)`` (1-based; 1 beyond ndims)."""
     return int(t.shape[k - 1]) if k <= t.dim() else 1
