@@ -465,28 +465,52 @@ unsigned pp_device_status(int reset) { return pp::read_device_status(reset != 0)
 // ---------------------------------------------------------------------------
 namespace {
 
+// Per-thread device workspace of the host-pointer layer: a grow-only buffer and
+// three streams (host-to-device copies, kernels, device-to-host copies) with
+// per-slab events, so the copies of one slab overlap the kernels of another.
+constexpr int kSlabs = 8;
 struct HostWorkspace {
     int device = -1;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;   // kernels
+    cudaStream_t h2d = nullptr;
+    cudaStream_t d2h = nullptr;
+    cudaEvent_t in_ready = nullptr;          // inputs shared by every slab are on the device
+    cudaEvent_t slab_in[kSlabs] = {};        // slab inputs copied
+    cudaEvent_t slab_out[kSlabs] = {};       // slab computed
     void* buf = nullptr;
     size_t cap = 0;
-    ~HostWorkspace() {
+    void release() {
         if (buf) cudaFree(buf);
-        if (stream) cudaStreamDestroy(stream);
+        for (cudaStream_t* st : {&stream, &h2d, &d2h})
+            if (*st) cudaStreamDestroy(*st);
+        if (in_ready) cudaEventDestroy(in_ready);
+        for (int k = 0; k < kSlabs; ++k) {
+            if (slab_in[k]) cudaEventDestroy(slab_in[k]);
+            if (slab_out[k]) cudaEventDestroy(slab_out[k]);
+            slab_in[k] = slab_out[k] = nullptr;
+        }
+        buf = nullptr;
+        cap = 0;
+        stream = h2d = d2h = nullptr;
+        in_ready = nullptr;
     }
+    ~HostWorkspace() { release(); }
     int reserve(size_t bytes) {
         int dev = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e != cudaSuccess) return pp::cuda_fail(e, "cudaGetDevice");
         if (dev != device) {
-            if (buf) cudaFree(buf);
-            if (stream) cudaStreamDestroy(stream);
-            buf = nullptr;
-            cap = 0;
-            stream = nullptr;
+            release();
             device = dev;
-            e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
-            if (e != cudaSuccess) return pp::cuda_fail(e, "cudaStreamCreate");
+            for (cudaStream_t* st : {&stream, &h2d, &d2h})
+                if ((e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking)) != cudaSuccess)
+                    return pp::cuda_fail(e, "cudaStreamCreate");
+            if ((e = cudaEventCreateWithFlags(&in_ready, cudaEventDisableTiming)) != cudaSuccess)
+                return pp::cuda_fail(e, "cudaEventCreate");
+            for (int k = 0; k < kSlabs; ++k)
+                if ((e = cudaEventCreateWithFlags(&slab_in[k], cudaEventDisableTiming)) != cudaSuccess ||
+                    (e = cudaEventCreateWithFlags(&slab_out[k], cudaEventDisableTiming)) != cudaSuccess)
+                    return pp::cuda_fail(e, "cudaEventCreate");
         }
         if (bytes > cap) {
             if (buf) cudaFree(buf);
@@ -507,7 +531,31 @@ void report(const char* fn, int rc) {
     if (rc != PP_OK) std::fprintf(stderr, "pushpull_gb300: %s failed (%d): %s\n", fn, rc, pp_last_error());
 }
 
-// kind: 0 pull, 1 pullg, 2 pullh, 3 push, 4 pushg
+// The host ABI passes the samples as a flat list of n1 voxels.  Each voxel is
+// computed independently, so any grid shape with n1 voxels gives the same
+// result; the shape only decides how voxels are grouped into tiles.  Samples on
+// the image grid (the usual case) are given that grid's shape so the tiled
+// kernels apply; otherwise the largest image-like factorisation is used.
+void infer_sample_grid(const pp_usize* d0, pp_usize n1, pp_usize d1[3]) {
+    const pp_usize plane = d0[0] * d0[1];
+    if (plane > 0 && n1 % plane == 0) {
+        d1[0] = d0[0];
+        d1[1] = d0[1];
+        d1[2] = n1 / plane;
+    } else if (d0[0] > 0 && n1 % d0[0] == 0) {
+        d1[0] = d0[0];
+        d1[1] = n1 / d0[0];
+        d1[2] = 1;
+    } else {
+        d1[0] = n1;
+        d1[1] = d1[2] = 1;
+    }
+}
+
+// kind: 0 pull, 1 pullg, 2 pullh, 3 push, 4 pushg.  The sample grid is cut into
+// up to kSlabs z-slabs: slab k's inputs are copied (h2d stream) while slab k-1
+// is computed (kernel stream) and slab k-2's results are copied back (d2h
+// stream).  Every copy is one cudaMemcpyAsync of a contiguous range.
 int compat_call(int kind, float* out, const float* phi, const float* in, const pp_usize* d0, pp_usize n1,
                 const int* bnd, const pp_usize* dp, int ext) {
     if (!d0 || !bnd || !dp) return pp::fail(PP_ERR_NULL, "d0, bnd and dp must not be NULL");
@@ -518,8 +566,10 @@ int compat_call(int kind, float* out, const float* phi, const float* in, const p
         b[k] = (bnd[k] >= 0 && bnd[k] <= 2) ? bnd[k] : 1;   // other codes act as reflect (patch.cu:55-57)
     }
     if (n1 == 0) return PP_OK;
+    if (!out || !phi || !in) return pp::fail(PP_ERR_NULL, "data pointers must not be NULL");
     const pp_usize n0 = d0[0] * d0[1] * d0[2];
-    const pp_usize d1[3] = {n1, 1, 1};
+    pp_usize d1[3];
+    infer_sample_grid(d0, n1, d1);
     const bool is_push = kind >= 3;
     const size_t comps_in = kind == 4 ? 3 : 1;
     const size_t comps_out = kind == 1 ? 3 : (kind == 2 ? 9 : 1);
@@ -532,28 +582,67 @@ int compat_call(int kind, float* out, const float* phi, const float* in, const p
     float* dphi = (float*)base;
     float* din = (float*)(base + round256(phi_b));
     float* dout = (float*)(base + round256(phi_b) + round256(in_b));
-    cudaStream_t s = g_ws.stream;
+    HostWorkspace& w = g_ws;
     cudaError_t e;
-    if ((e = cudaMemcpyAsync(dphi, phi, phi_b, cudaMemcpyHostToDevice, s)) != cudaSuccess)
-        return pp::cuda_fail(e, "copy phi");
-    if ((e = cudaMemcpyAsync(din, in, in_b, cudaMemcpyHostToDevice, s)) != cudaSuccess)
-        return pp::cuda_fail(e, "copy input");
-    if (is_push && (e = cudaMemcpyAsync(dout, out, out_b, cudaMemcpyHostToDevice, s)) != cudaSuccess)
-        return pp::cuda_fail(e, "copy accumulator");
-    switch (kind) {
-        case 0: rc = pp_pull(dout, dphi, din, d0, d1, 1, 1, b, 1, deg, ext, s); break;
-        case 1: rc = pp_pull_grad(dout, dphi, din, d0, d1, 1, 1, b, 1, deg, ext, s); break;
-        case 2: rc = pp_pull_hess(dout, dphi, din, d0, d1, 1, 1, b, 1, deg, ext, s); break;
-        case 3: rc = pp_push(dout, dphi, din, d0, d1, 1, 1, b, 1, deg, ext, 1, s); break;
-        default: rc = pp_push_grad(dout, dphi, din, d0, d1, 1, 1, b, 1, deg, ext, 1, s); break;
+    // inputs every slab needs: the image (pull family) or the accumulator (push family)
+    if (is_push) e = cudaMemcpyAsync(dout, out, out_b, cudaMemcpyHostToDevice, w.h2d);
+    else e = cudaMemcpyAsync(din, in, in_b, cudaMemcpyHostToDevice, w.h2d);
+    if (e != cudaSuccess) return pp::cuda_fail(e, "copy shared input");
+    if ((e = cudaEventRecord(w.in_ready, w.h2d)) != cudaSuccess) return pp::cuda_fail(e, "event");
+    if ((e = cudaStreamWaitEvent(w.stream, w.in_ready, 0)) != cudaSuccess) return pp::cuda_fail(e, "wait");
+    // slabs of whole z-planes, at least 1 Mi voxels each
+    const pp_usize plane = d1[0] * d1[1];
+    pp_usize nslab = d1[2] < (pp_usize)kSlabs ? d1[2] : (pp_usize)kSlabs;
+    while (nslab > 1 && (d1[2] / nslab) * plane < (1u << 20)) --nslab;
+    if (nslab < 1) nslab = 1;
+    for (pp_usize k = 0; k < nslab; ++k) {
+        const pp_usize z0 = d1[2] * k / nslab, z1 = d1[2] * (k + 1) / nslab;
+        const pp_usize off = z0 * plane, ns = (z1 - z0) * plane;
+        if (ns == 0) continue;
+        // slab inputs, compact: phi (ns, 3) at dphi + 3 off; push values (ns, comps) at din + comps off
+        float* sphi = dphi + 3 * off;
+        for (int c = 0; c < 3; ++c)
+            if ((e = cudaMemcpyAsync(sphi + c * ns, phi + c * n1 + off, ns * sizeof(float), cudaMemcpyHostToDevice,
+                                     w.h2d)) != cudaSuccess)
+                return pp::cuda_fail(e, "copy phi slab");
+        float* sin = is_push ? din + comps_in * off : din;
+        if (is_push)
+            for (size_t c = 0; c < comps_in; ++c)
+                if ((e = cudaMemcpyAsync(sin + c * ns, in + c * n1 + off, ns * sizeof(float),
+                                         cudaMemcpyHostToDevice, w.h2d)) != cudaSuccess)
+                    return pp::cuda_fail(e, "copy value slab");
+        if ((e = cudaEventRecord(w.slab_in[k], w.h2d)) != cudaSuccess) return pp::cuda_fail(e, "event");
+        if ((e = cudaStreamWaitEvent(w.stream, w.slab_in[k], 0)) != cudaSuccess) return pp::cuda_fail(e, "wait");
+        const pp_usize sd1[3] = {d1[0], d1[1], z1 - z0};
+        float* sout = is_push ? dout : dout + comps_out * off;
+        switch (kind) {
+            case 0: rc = pp_pull(sout, sphi, din, d0, sd1, 1, 1, b, 1, deg, ext, w.stream); break;
+            case 1: rc = pp_pull_grad(sout, sphi, din, d0, sd1, 1, 1, b, 1, deg, ext, w.stream); break;
+            case 2: rc = pp_pull_hess(sout, sphi, din, d0, sd1, 1, 1, b, 1, deg, ext, w.stream); break;
+            case 3: rc = pp_push(sout, sphi, sin, d0, sd1, 1, 1, b, 1, deg, ext, 1, w.stream); break;
+            default: rc = pp_push_grad(sout, sphi, sin, d0, sd1, 1, 1, b, 1, deg, ext, 1, w.stream); break;
+        }
+        if (rc != PP_OK) {
+            for (cudaStream_t st : {w.h2d, w.stream, w.d2h}) cudaStreamSynchronize(st);
+            return rc;
+        }
+        if (!is_push) {
+            if ((e = cudaEventRecord(w.slab_out[k], w.stream)) != cudaSuccess) return pp::cuda_fail(e, "event");
+            if ((e = cudaStreamWaitEvent(w.d2h, w.slab_out[k], 0)) != cudaSuccess) return pp::cuda_fail(e, "wait");
+            for (size_t c = 0; c < comps_out; ++c)
+                if ((e = cudaMemcpyAsync(out + c * n1 + off, sout + c * ns, ns * sizeof(float),
+                                         cudaMemcpyDeviceToHost, w.d2h)) != cudaSuccess)
+                    return pp::cuda_fail(e, "copy result slab");
+        }
     }
-    if (rc != PP_OK) {
-        cudaStreamSynchronize(s);
-        return rc;
+    if (is_push) {
+        if ((e = cudaEventRecord(w.slab_out[0], w.stream)) != cudaSuccess) return pp::cuda_fail(e, "event");
+        if ((e = cudaStreamWaitEvent(w.d2h, w.slab_out[0], 0)) != cudaSuccess) return pp::cuda_fail(e, "wait");
+        if ((e = cudaMemcpyAsync(out, dout, out_b, cudaMemcpyDeviceToHost, w.d2h)) != cudaSuccess)
+            return pp::cuda_fail(e, "copy result");
     }
-    if ((e = cudaMemcpyAsync(out, dout, out_b, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
-        return pp::cuda_fail(e, "copy result");
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return pp::cuda_fail(e, "synchronize");
+    for (cudaStream_t st : {w.h2d, w.stream, w.d2h})
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return pp::cuda_fail(e, "synchronize");
     return PP_OK;
 }
 
@@ -577,7 +666,7 @@ int compat_affine(bool push, float* out, const float* in, const pp_usize* d0, pp
     if (rc != PP_OK) return rc;
     float* din = (float*)g_ws.buf;
     float* dout = (float*)((char*)g_ws.buf + round256(in_b));
-    cudaStream_t s = g_ws.stream;
+    cudaStream_t s = g_ws.stream;   // the affine calls run on the kernel stream alone
     cudaError_t e;
     if ((e = cudaMemcpyAsync(din, in, in_b, cudaMemcpyHostToDevice, s)) != cudaSuccess)
         return pp::cuda_fail(e, "copy input");
