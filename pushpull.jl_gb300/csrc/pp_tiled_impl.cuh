@@ -183,19 +183,22 @@ __device__ __forceinline__ void reduce_box(int (&mn)[3], int (&mx)[3], const Til
         red[warp][6] = __float_as_int(ssum);
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (warp == 0) {
+        // warp 0 combines the per-warp records (lane w < 8 holds warp w's)
+        constexpr int NW = kThreads / 32;
+        int lo[3], hi[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = __reduce_min_sync(0xffffffffu, lane < NW ? red[lane][k] : INT_MAX);
+            hi[k] = __reduce_max_sync(0xffffffffu, lane < NW ? red[lane][3 + k] : INT_MIN);
+        }
+        // the scale bound is summed in a fixed order (warp 0, 1, ...): lane 0 alone
         float S = 0.f;
-        for (int w = 0; w < kThreads / 32; ++w) S += __int_as_float(red[w][6]);
+        if (lane == 0)
+            for (int w = 0; w < NW; ++w) S += __int_as_float(red[w][6]);
+        if (lane == 0) {
         box.S = S;
         box.E = scale_exponent(S);
-        int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
-#pragma unroll
-        for (int w = 0; w < kThreads / 32; ++w)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                lo[k] = min(lo[k], red[w][k]);
-                hi[k] = max(hi[k], red[w][3 + k]);
-            }
         if (lo[0] > hi[0]) {
             box.mode = 0;
             box.tma = 0;
@@ -242,6 +245,7 @@ __device__ __forceinline__ void reduce_box(int (&mn)[3], int (&mx)[3], const Til
             box.Q = staged ? (int)Q : 0;
             box.size = staged ? (int)size : 0;
             box.interior = interior;
+        }
         }
     }
     __syncthreads();
@@ -610,62 +614,114 @@ __device__ __forceinline__ void tile_bounds(const Geometry& g, const TileOrigin&
 // The patch contraction of contract() (pp_voxel.cuh) with the z loop rolled:
 // the z weights rotate through slot 0 and `next()` advances the loader to the
 // next plane, so only one plane of rows is in flight (a fully unrolled patch
-// needs more registers than two resident CTAs per SM leave).  `row(j, f)` loads
-// row j of the current plane into f[0..DP).
+// needs more registers than two resident CTAs per SM leave).  Rows are taken in
+// pairs on the packed f32x2 pipe.  `row(j, f)` loads row j of the current plane
+// into f[0..DP).
 template <int OP, int DP, class WT, class ROW, class NEXT>
 __device__ __forceinline__ void contract_rolled(const WT& ax, const WT& ay, WT az, ROW row, NEXT next,
                                                 float (&r)[6]) {
+    constexpr int ORD = op_order(OP);
+    constexpr int NJ = OP == kPull ? 1 : (ORD == 1 ? 3 : 6);   // y-level accumulators
 #pragma unroll
     for (int q = 0; q < 6; ++q) r[q] = 0.f;
-#pragma unroll 1
-    for (int k = 0; k < DP; ++k) {
-        float j0 = 0.f, j1 = 0.f, j2 = 0.f, j3 = 0.f, j4 = 0.f, j5 = 0.f;
+    // x weights duplicated into f32x2 pairs once: rows are contracted two at a
+    // time on the packed pipe (lane 0: row j, lane 1: row j + 1)
+    float2 wx2[DP], dwx2[ORD >= 1 ? DP : 1], hwx2[ORD >= 2 ? DP : 1];
 #pragma unroll
-        for (int j = 0; j < DP; ++j) {
+    for (int i = 0; i < DP; ++i) {
+        wx2[i] = make_float2(ax.w[i], ax.w[i]);
+        if constexpr (ORD >= 1) dwx2[i] = make_float2(ax.dw[i], ax.dw[i]);
+        if constexpr (ORD >= 2) hwx2[i] = make_float2(ax.hw[i], ax.hw[i]);
+    }
+    // pull keeps two planes in flight; the derivative ops, with more
+    // accumulators, one (two would need more registers than 2 CTAs/SM leave)
+    constexpr int KU = OP == kPull ? 2 : 1;
+#pragma unroll KU
+    for (int k = 0; k < DP; ++k) {
+        float2 J[NJ];
+#pragma unroll
+        for (int q = 0; q < NJ; ++q) J[q] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j + 1 < DP; j += 2) {
+            float fa[DP], fb[DP];
+            row(j, fa);
+            row(j + 1, fb);
+            float2 I0 = make_float2(0.f, 0.f), I1 = I0, I2 = I0;
+#pragma unroll
+            for (int i = 0; i < DP; ++i) {
+                const float2 f2 = make_float2(fa[i], fb[i]);
+                I0 = __ffma2_rn(wx2[i], f2, I0);
+                if constexpr (ORD >= 1) I1 = __ffma2_rn(dwx2[i], f2, I1);
+                if constexpr (ORD >= 2) I2 = __ffma2_rn(hwx2[i], f2, I2);
+            }
+            const float2 wy = make_float2(ay.w[j], ay.w[j + 1]);
+            if constexpr (OP == kPull) {
+                J[0] = __ffma2_rn(wy, I0, J[0]);
+            } else if constexpr (ORD == 1) {
+                const float2 dwy = make_float2(ay.dw[j], ay.dw[j + 1]);
+                J[0] = __ffma2_rn(wy, I1, J[0]);
+                J[1] = __ffma2_rn(dwy, I0, J[1]);
+                J[2] = __ffma2_rn(wy, I0, J[2]);
+            } else {
+                const float2 dwy = make_float2(ay.dw[j], ay.dw[j + 1]);
+                const float2 hwy = make_float2(ay.hw[j], ay.hw[j + 1]);
+                J[0] = __ffma2_rn(wy, I2, J[0]);
+                J[1] = __ffma2_rn(hwy, I0, J[1]);
+                J[2] = __ffma2_rn(wy, I0, J[2]);
+                J[3] = __ffma2_rn(dwy, I1, J[3]);
+                J[4] = __ffma2_rn(wy, I1, J[4]);
+                J[5] = __ffma2_rn(dwy, I0, J[5]);
+            }
+        }
+        if constexpr (DP & 1) {   // the last row alone, into lane 0
+            constexpr int j = DP - 1;
             float f[DP];
             row(j, f);
             float i0 = 0.f, i1 = 0.f, i2 = 0.f;
 #pragma unroll
             for (int i = 0; i < DP; ++i) {
                 i0 = fmaf(ax.w[i], f[i], i0);
-                if constexpr (op_order(OP) >= 1) i1 = fmaf(ax.dw[i], f[i], i1);
-                if constexpr (op_order(OP) >= 2) i2 = fmaf(ax.hw[i], f[i], i2);
+                if constexpr (ORD >= 1) i1 = fmaf(ax.dw[i], f[i], i1);
+                if constexpr (ORD >= 2) i2 = fmaf(ax.hw[i], f[i], i2);
             }
             if constexpr (OP == kPull) {
-                j0 = fmaf(ay.w[j], i0, j0);
-            } else if constexpr (OP == kPullGrad || OP == kPullValGrad) {
-                j0 = fmaf(ay.w[j], i1, j0);
-                j1 = fmaf(ay.dw[j], i0, j1);
-                j2 = fmaf(ay.w[j], i0, j2);
+                J[0].x = fmaf(ay.w[j], i0, J[0].x);
+            } else if constexpr (ORD == 1) {
+                J[0].x = fmaf(ay.w[j], i1, J[0].x);
+                J[1].x = fmaf(ay.dw[j], i0, J[1].x);
+                J[2].x = fmaf(ay.w[j], i0, J[2].x);
             } else {
-                j0 = fmaf(ay.w[j], i2, j0);
-                j1 = fmaf(ay.hw[j], i0, j1);
-                j2 = fmaf(ay.w[j], i0, j2);
-                j3 = fmaf(ay.dw[j], i1, j3);
-                j4 = fmaf(ay.w[j], i1, j4);
-                j5 = fmaf(ay.dw[j], i0, j5);
+                J[0].x = fmaf(ay.w[j], i2, J[0].x);
+                J[1].x = fmaf(ay.hw[j], i0, J[1].x);
+                J[2].x = fmaf(ay.w[j], i0, J[2].x);
+                J[3].x = fmaf(ay.dw[j], i1, J[3].x);
+                J[4].x = fmaf(ay.w[j], i1, J[4].x);
+                J[5].x = fmaf(ay.dw[j], i0, J[5].x);
             }
         }
+        float jv[NJ];
+#pragma unroll
+        for (int q = 0; q < NJ; ++q) jv[q] = J[q].x + J[q].y;
         if constexpr (OP == kPull) {
-            r[0] = fmaf(az.w[0], j0, r[0]);
-        } else if constexpr (OP == kPullGrad || OP == kPullValGrad) {
-            r[0] = fmaf(az.w[0], j0, r[0]);
-            r[1] = fmaf(az.w[0], j1, r[1]);
-            r[2] = fmaf(az.dw[0], j2, r[2]);
-            if constexpr (OP == kPullValGrad) r[3] = fmaf(az.w[0], j2, r[3]);
+            r[0] = fmaf(az.w[0], jv[0], r[0]);
+        } else if constexpr (ORD == 1) {
+            r[0] = fmaf(az.w[0], jv[0], r[0]);
+            r[1] = fmaf(az.w[0], jv[1], r[1]);
+            r[2] = fmaf(az.dw[0], jv[2], r[2]);
+            if constexpr (OP == kPullValGrad) r[3] = fmaf(az.w[0], jv[2], r[3]);
         } else {
-            r[0] = fmaf(az.w[0], j0, r[0]);
-            r[1] = fmaf(az.w[0], j1, r[1]);
-            r[2] = fmaf(az.hw[0], j2, r[2]);
-            r[3] = fmaf(az.w[0], j3, r[3]);
-            r[4] = fmaf(az.dw[0], j4, r[4]);
-            r[5] = fmaf(az.dw[0], j5, r[5]);
+            r[0] = fmaf(az.w[0], jv[0], r[0]);
+            r[1] = fmaf(az.w[0], jv[1], r[1]);
+            r[2] = fmaf(az.hw[0], jv[2], r[2]);
+            r[3] = fmaf(az.w[0], jv[3], r[3]);
+            r[4] = fmaf(az.dw[0], jv[4], r[4]);
+            r[5] = fmaf(az.dw[0], jv[5], r[5]);
         }
 #pragma unroll
         for (int i = 0; i + 1 < DP; ++i) {
             az.w[i] = az.w[i + 1];
-            if constexpr (op_order(OP) >= 1) az.dw[i] = az.dw[i + 1];
-            if constexpr (op_order(OP) >= 2) az.hw[i] = az.hw[i + 1];
+            if constexpr (ORD >= 1) az.dw[i] = az.dw[i + 1];
+            if constexpr (ORD >= 2) az.hw[i] = az.hw[i + 1];
         }
         next();
     }

@@ -76,7 +76,10 @@ def test_host_symbols_pipelined_match_native(pkg, O, d0, d1):
     out1 = np.zeros(d1, dtype=np.float32, order="F")
     _host_call(lib, "pull", out1, phi, f0, d0, n1, (1, 1, 1), (3, 3, 3), 1)
     ref1 = L.to_numpy(pkg.pull(L.from_numpy(f0), L.from_numpy(phi), s))
-    assert np.array_equal(out1, ref1)
+    # the same kernels when the grid is inferred exactly; otherwise the per-voxel
+    # kernels, whose summation order differs from the tiled ones
+    exact = tuple(d0) == tuple(d1)
+    assert np.array_equal(out1, ref1) if exact else rel_err(out1, ref1) <= 1e-6
     acc = np.full(d0, 0.5, dtype=np.float32, order="F")            # push adds into the caller's array
     _host_call(lib, "push", acc, phi, f1, d0, n1, (1, 1, 1), (3, 3, 3), 1)
     ref0 = L.to_numpy(pkg.push(L.from_numpy(f1), L.from_numpy(phi), d0, s)) + np.float32(0.5)
@@ -84,7 +87,8 @@ def test_host_symbols_pipelined_match_native(pkg, O, d0, d1):
     g = np.asfortranarray(rng.standard_normal(d1 + (3,)).astype(np.float32))
     outg = np.zeros(d1 + (3,), dtype=np.float32, order="F")
     _host_call(lib, "pullg", outg, phi, f0, d0, n1, (1, 1, 1), (3, 3, 3), 1)
-    assert np.array_equal(outg, L.to_numpy(pkg.pull_grad(L.from_numpy(f0), L.from_numpy(phi), s)))
+    refg = L.to_numpy(pkg.pull_grad(L.from_numpy(f0), L.from_numpy(phi), s))
+    assert np.array_equal(outg, refg) if exact else rel_err(outg, refg) <= 1e-6
     accg = np.zeros(d0, dtype=np.float32, order="F")
     _host_call(lib, "pushg", accg, phi, g, d0, n1, (1, 1, 1), (3, 3, 3), 1)
     assert rel_err(accg, L.to_numpy(pkg.push_grad(L.from_numpy(g), L.from_numpy(phi), d0, s))) <= 1e-5
