@@ -209,18 +209,21 @@ enum pp_path { PP_PATH_AUTO = 0, PP_PATH_DIRECT = 1 };
 
 /* Tile of sample voxels per CTA (2^lx x 2^ly x 2^lz, 32..512 voxels) and the
  * shared-memory budget of its image footprint box in floats, for one op
- * (-1: all ops) and one isotropic degree (-1: all degrees).  No reference
- * counterpart (the reference launches one thread per voxel with no tiling,
- * ext/pushpull_gpu.jl:386-391); used by the autotuner. */
+ * (-1: all ops) and one isotropic degree (-1: all degrees).  cap_floats == 0
+ * selects the per-voxel kernels for that (op, degree); this is the default for
+ * degrees 0 and 1, where gathering straight from L2 beats staging a box.  No
+ * reference counterpart (the reference launches one thread per voxel with no
+ * tiling, ext/pushpull_gpu.jl:386-391); used by the autotuner. */
 int pp_set_tile(int op, int deg, int lx, int ly, int lz, int cap_floats);
 int pp_get_tile(int op, int deg, int *lx, int *ly, int *lz, int *cap_floats);
 /* Autotuner: times the per-voxel kernels and every candidate tile shape and
  * shared-memory budget for op (PP_OP_PULL .. PP_OP_PUSH_GRAD) on the caller's
  * own arguments (same meaning as the op's entry point; push ops run with
  * accumulate = 0, so out is overwritten), reps timed runs each with CUDA
- * events, installs the best tiled configuration for (op, deg[0]) and returns
- * best = {lx, ly, lz, cap, path} (path PP_PATH_DIRECT when the per-voxel
- * kernels were fastest) and its mean time in ms.  Synchronises the stream. */
+ * events, installs the fastest configuration for (op, deg[0]) (cap 0 when the
+ * per-voxel kernels won) and returns best = {lx, ly, lz, cap, path} (path
+ * PP_PATH_DIRECT when the per-voxel kernels were fastest) and its mean time in
+ * ms.  Synchronises the stream. */
 int pp_autotune(int op, float *out, const float *phi, const float *in, const pp_usize d0[3], const pp_usize d1[3],
                 int nc, int nb, const int *bnd, int nbnd, const int deg[3], int ext, int reps, void *stream,
                 int *best, float *best_ms);

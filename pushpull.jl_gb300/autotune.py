@@ -69,15 +69,16 @@ def tune(op: str, x: torch.Tensor, phi: torch.Tensor, sett: Settings, d0=None, r
 
 
 def load() -> int:
-    """Install every cached tiled choice of this device; returns how many."""
+    """Install every cached choice of this device; returns how many."""
     lib = _native.lib()
     dev = torch.cuda.get_device_name()
     n = 0
     for key, res in _read().items():
         d, op, deg, _ = key.split("|")
-        if d != dev or res.get("path") != "tiled":
+        if d != dev:
             continue
         lx, ly, lz = res["tile"]
-        if lib.pp_set_tile(OPS[op], int(deg[3:]), lx, ly, lz, res["cap"]) == 0:
+        cap = res["cap"] if res.get("path") == "tiled" else 0     # cap 0: per-voxel kernels
+        if lib.pp_set_tile(OPS[op], int(deg[3:]), lx, ly, lz, cap) == 0:
             n += 1
     return n

@@ -77,6 +77,8 @@ __device__ __forceinline__ long long fold_tap(int bnd, long long i, long long d,
     sign = 1.0f;
     if (i >= 0 && i < d) return i;
     if (bnd == 0) {
+        if (i < 0 && i >= -d) return i + d;   // one period either side: no 64-bit modulo
+        if (i >= d && i < 2 * d) return i - d;
         long long r = i % d;
         return r < 0 ? r + d : r;
     }

@@ -137,9 +137,10 @@ def test_autotune_installs_valid_choice(pkg, O, restore_tiles, tmp_path, monkeyp
     for op, x in [("pull", f0), ("push", f0)]:
         res = A.tune(op, L.from_numpy(x), L.from_numpy(phi), s, d0=d0, reps=2)
         assert res["path"] in ("tiled", "direct") and res["ms"] > 0
-        assert sum(res["tile"]) >= 6 and res["cap"] >= 4096
+        assert sum(res["tile"]) >= 6
+        assert res["cap"] >= 4096 if res["path"] == "tiled" else res["cap"] == 0
     got1 = L.to_numpy(pkg.pull(L.from_numpy(f0), L.from_numpy(phi), s))
     got0 = L.to_numpy(pkg.push(L.from_numpy(f0), L.from_numpy(phi), d0, s))
     assert rel_err(got1, O.pull(f0, phi, so)) <= 1e-5
     assert rel_err(got0, O.push(f0, phi, d0, so)) <= 1e-4
-    assert A.load() == sum(1 for v in __import__("json").load(open(A.CACHE)).values() if v["path"] == "tiled")
+    assert A.load() == len(__import__("json").load(open(A.CACHE)))
