@@ -96,14 +96,15 @@ int g_path = PP_PATH_AUTO;
 
 void init_tiles_locked() {
     if (g_tiles_init) return;
-    // 8x8x8 tiles; the push family keeps two words per accumulator element.
+    // 8x8x8 tiles; the push family keeps two words per accumulator element; the
+    // fused step's 2560-float budget at degree 2 leaves room for three CTAs per SM.
     // Degrees 0 and 1 (one or two taps per axis) default to the per-voxel
     // kernels (cap 0): with so few taps, gathering through L2 is faster than
     // staging a footprint box (192^3, GB300: pull 0.10 vs 0.16 ms, push 0.13 vs
     // 0.24 ms, fused step 0.29 vs 0.40 ms at degree 1).
     for (int op = 0; op < 6; ++op)
         for (int d = 0; d < 5; ++d)
-            g_tiles[op][d] = TileCfg{3, 3, 3, d <= 1 ? 0 : (op < 3 ? 8192 : (op < 5 ? 16384 : 4096))};
+            g_tiles[op][d] = TileCfg{3, 3, 3, d <= 1 ? 0 : (op < 3 ? 8192 : (op < 5 ? 16384 : (d == 2 ? 2560 : 4096)))};
     g_tiles_init = true;
 }
 }  // namespace

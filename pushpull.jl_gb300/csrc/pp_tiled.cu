@@ -51,8 +51,15 @@ cudaError_t launch_push_tiled(int op, const LaunchArgs& a, const TileCfg& t, cud
 
 int fused_tiled_grid(const LaunchArgs& a, const TileCfg& c) {
     const TileGrid t = make_grid(a, c);
-    // two CTAs per SM: the shared memory (ring, box, accumulator) admits two
-    const long long want = 2LL * sm_count();
+    // every CTA resident at once: as many per SM as the shared memory (ring,
+    // two box buffers, two-word accumulator) admits, at most what the kernel's
+    // register budget allows (three up to degree 2, two above)
+    const int nv = (1 << (c.lx + c.ly + c.lz)) > kThreads ? 2 * kThreads : kThreads;
+    const long long smem = (long long)kStages * 4 * nv * 4 + 4LL * c.cap * 4 + 8 * kStages + 1024;
+    const long long reg_cap = a.g.dp[0] <= 3 ? 3 : 2;
+    long long per_sm = (228LL * 1024) / smem;
+    per_sm = per_sm < 1 ? 1 : (per_sm > reg_cap ? reg_cap : per_sm);
+    const long long want = per_sm * sm_count();
     return (int)(t.ntiles < want ? t.ntiles : want);
 }
 

@@ -1302,7 +1302,7 @@ __device__ __forceinline__ float fused_voxel_global(const LaunchArgs& a, int b, 
 }
 
 template <int DP, int V, typename IT, bool TMA>
-__global__ void __launch_bounds__(kThreads, 2) k_fused_tiled(const __grid_constant__ LaunchArgs a,
+__global__ void __launch_bounds__(kThreads, DP <= 3 ? 3 : 2) k_fused_tiled(const __grid_constant__ LaunchArgs a,
                                                              const __grid_constant__ TileGrid t,
                                                              const __grid_constant__ CUtensorMap phimap,
                                                              const __grid_constant__ CUtensorMap gmap) {
