@@ -46,7 +46,7 @@ def _peaks():
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each kernel
 # on this workload, from one ncu capture (profiles/k_pull_tiled_192cubic.md, profiles/k_push_tiled_192cubic.md).
-TRAFFIC = {"pull": 129_179_904, "push": 152_983_808}
+TRAFFIC = {"pull": 126_790_144, "push": 152_880_128}
 
 
 class Clocks:
