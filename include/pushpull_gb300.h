@@ -114,6 +114,18 @@ int pp_push_grad(float *g0, const float *phi, const float *g1,
                  const int *bnd, int nbnd, const int deg[3], int ext,
                  int accumulate, void *stream);
 
+/* f0 (+)= push(f1, phi) and c0 (+)= push(1, phi) in one pass: the count image
+ * holds the (signed) weight each image voxel received, from the same voxels
+ * as f0 (non-finite f1 values and invalid voxels contribute to neither).
+ * Replaces pushc_element (artifacts/C/pushpull.cu:128-142; push1 with c0,
+ * pushpull_dev.cu:140-154), which normalised multigrid restriction needs
+ * (src/multigrid.jl:26-31 pushes the values, then ones).  c0 has the layout of
+ * f0.  Per-voxel kernel with global reductions. */
+int pp_push_count(float *f0, float *c0, const float *phi, const float *f1,
+                  const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
+                  const int *bnd, int nbnd, const int deg[3], int ext,
+                  int accumulate, void *stream);
+
 /* Fused forward + adjoint step of the loss sum((pull(f0, phi) - g)^2):
  *   *loss (device double) = sum over batch, channel and voxel of r^2, r = pull(f0, phi) - g
  *   df   (d0, nc, nb)  (+)= push(2 r, phi)               -- the f0 cotangent

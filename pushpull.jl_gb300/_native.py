@@ -49,6 +49,8 @@ _SIGS = {
                                _i32x3, C.c_int, C.c_int, _vp]),
     "pp_fused_step": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int,
                                 _i32x3, C.c_int, C.c_int, _vp]),
+    "pp_push_count": (C.c_int, [_vp, _vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int, _i32x3,
+                                C.c_int, C.c_int, _vp]),
     "pp_fused_step_noalloc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp,
                                         C.c_int, _i32x3, C.c_int, C.c_int, _vp]),
     "pp_pull_affine": (C.c_int, [_vp, _vp, _vp, _u64x3, _u64x3, C.c_int, C.c_int, _vp, C.c_int, _i32x3, C.c_int,

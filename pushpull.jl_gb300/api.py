@@ -129,6 +129,33 @@ def push_grad(g1: torch.Tensor, phi: torch.Tensor, d0, sett: Settings = Settings
     return _push_family("pp_push_grad", g1, phi, d0, sett, True, out, accumulate)
 
 
+def push_count(f1: torch.Tensor, phi: torch.Tensor, d0, sett: Settings = Settings(), *, out=None, count=None,
+               accumulate: bool = False):
+    """``(push(f₁, ϕ), push(1, ϕ))`` in one pass: the pushed values and the
+    weight every image voxel received from the same (finite, valid) samples
+    (the reference's ``pushc``, artifacts/C/pushpull.cu:128-142)."""
+    assert 3 <= f1.dim() <= 5, "`f₁` must have between 3 & 5 dimensions"
+    assert 4 <= phi.dim() <= 5 and L.jsize(phi, 4) == 3
+    assert L.jsize(phi, 5) == L.jsize(f1, 5) and tuple(f1.shape[:3]) == tuple(phi.shape[:3])
+    nc, nb = L.jsize(f1, 4), L.jsize(f1, 5)
+    assert len(sett.bnd) == nc or len(sett.bnd) == 1
+    _require_cuda(f1, phi)
+    f1, phi = L.colmajor(f1), L.colmajor(phi)
+    d0 = tuple(int(v) for v in d0)
+    shape = d0 + tuple(f1.shape[3:])
+    if out is None or count is None:
+        out, count, accumulate = L.empty(shape, device=f1.device), L.empty(shape, device=f1.device), False
+    for t in (out, count):
+        _require_cuda(t)
+        assert tuple(t.shape) == shape and L.is_colmajor(t)
+    lib = _native.lib()
+    rc = lib.pp_push_count(out.data_ptr(), count.data_ptr(), phi.data_ptr(), f1.data_ptr(), _native.u64x3(d0),
+                           _native.u64x3(tuple(phi.shape[:3])), nc, nb, sett.bnd_array(), sett.nbnd,
+                           _native.i32x3(sett.deg), sett.ext, int(bool(accumulate)), _stream(f1))
+    _native.check("pp_push_count", rc)
+    return out, count
+
+
 def adjust_affine(Aff) -> list:
     """1-based 3x4 (or 4x4) affine -> 0-based 3x4, column-major as 12 floats
     (src/pushpull_cpu.jl:357-362: the last column becomes the row sums minus 1,

@@ -331,6 +331,27 @@ int pp_push_grad(float* g0, const float* phi, const float* g1, const pp_usize d0
     return run_push(pp::kPushGrad, g0, phi, g1, d0, d1, nc, nb, bnd, nbnd, deg, ext, accumulate, stream);
 }
 
+int pp_push_count(float* f0, float* c0, const float* phi, const float* f1, const pp_usize d0[3], const pp_usize d1[3],
+                  int nc, int nb, const int* bnd, int nbnd, const int deg[3], int ext, int accumulate, void* stream) {
+    using namespace pp;
+    LaunchArgs a{};
+    int rc = prepare(a, f0, phi, f1, d0, d1, nc, nb, bnd, nbnd, deg, ext);
+    if (rc != PP_OK) return rc;
+    if (!c0) return fail(PP_ERR_NULL, "count image pointer must not be NULL");
+    if (!aligned4(c0)) return fail(PP_ERR_ALIGN, "float pointers must be 4-byte aligned");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!accumulate && a.g.n0 > 0) {
+        const size_t bytes = (size_t)a.g.n0 * a.g.nc * a.g.nb * sizeof(float);
+        cudaError_t e = cudaMemsetAsync(f0, 0, bytes, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c0, 0, bytes, s);
+        if (e != cudaSuccess) return cuda_fail(e, "zero outputs");
+    }
+    if (a.g.n1 == 0) return PP_OK;
+    a.out2 = c0;
+    const cudaError_t e = launch_push_direct(kPush, a, s);
+    return e == cudaSuccess ? PP_OK : cuda_fail(e, "push_count launch");
+}
+
 int pp_fused_step(double* loss, float* df, float* dphi, const float* f0, const float* phi, const float* g,
                   const pp_usize d0[3], const pp_usize d1[3], int nc, int nb, const int* bnd, int nbnd,
                   const int deg[3], int ext, int accumulate, void* stream) {

@@ -29,7 +29,7 @@ struct LaunchArgs {
     float* out;         // pull: (d1, ncomp, nc, nb); push: (d0, nc, nb); dot ops: (d1, 3, nb)
     const float* up;    // dot ops: upstream, (d1, nc, nb) for GradDot, (d1, 3, nc, nb) for HessDot;
                         // fused step: the target g, (d1, nc, nb)
-    float* out2;        // fused step: deformation cotangent (d1, 3, nb)
+    float* out2;        // fused step: deformation cotangent (d1, 3, nb); push: count image or NULL
     double* partial;    // fused step: one loss partial per CTA
     const unsigned* fmax;   // fused step: max |f0| per (channel, batch), float bits
     Geometry g;

@@ -224,6 +224,8 @@ __device__ __forceinline__ void push_voxel_global(const LaunchArgs& a, int b, lo
             prev = code;
         }
         float* f0 = a.out + ((long long)b * g.nc + c) * g.n0;
+        // push with a count image (pushc): the weights alone go to out2 as well
+        float* c0 = OP == kPush && a.out2 ? a.out2 + ((long long)b * g.nc + c) * g.n0 : nullptr;
 #pragma unroll
         for (int k = 0; k < N; ++k) {
             if (DP == 0 && k >= az.n) break;
@@ -231,6 +233,17 @@ __device__ __forceinline__ void push_voxel_global(const LaunchArgs& a, int b, lo
             for (int j = 0; j < N; ++j) {
                 if (DP == 0 && j >= ay.n) break;
                 float* row = f0 + (az.off[k] + ay.off[j]);
+                if constexpr (OP == kPush) {
+                    if (c0) {
+                        const float wyz = ay.w[j] * az.w[k];
+                        float* crow = c0 + (az.off[k] + ay.off[j]);
+#pragma unroll
+                        for (int i = 0; i < N; ++i) {
+                            if (DP == 0 && i >= ax.n) break;
+                            atomicAdd(crow + ax.off[i], wyz * ax.w[i]);
+                        }
+                    }
+                }
                 float ca, cb;   // tap value = ca * dw_x + cb * w_x
                 if constexpr (OP == kPushGrad) {
                     ca = v0 * (ay.w[j] * az.w[k]);
