@@ -48,11 +48,6 @@ __device__ __forceinline__ float lds_f32(unsigned a) {
     asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
     return v;
 }
-__device__ __forceinline__ int lds_s32(unsigned a) {
-    int v;
-    asm volatile("ld.shared.s32 %0, [%1];" : "=r"(v) : "r"(a));
-    return v;
-}
 __device__ __forceinline__ void red_shared_s32(unsigned a, int v) {
     asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }

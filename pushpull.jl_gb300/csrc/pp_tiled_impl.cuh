@@ -377,16 +377,6 @@ struct FixedScale {
     }
 };
 
-// hi_addr / lo_addr: shared-window byte addresses of the element's two words
-__device__ __forceinline__ void fixed_add(unsigned hi_addr, unsigned lo_addr, float c, const FixedScale& fs) {
-    const float t1 = __fadd_rn(c * fs.inv_q1, kMagic);
-    const int h = __float_as_int(t1) - kMagicBits;
-    const float r = fmaf(-__fsub_rn(t1, kMagic), fs.q1, c);
-    const int l = __float_as_int(__fadd_rn(r * fs.inv_q2, kMagic)) - kMagicBits;
-    red_shared_s32(hi_addr, h);
-    red_shared_s32(lo_addr, l);
-}
-
 __device__ __forceinline__ float fixed_value(int h, int l, const FixedScale& fs) {
     return fmaf(__int2float_rn(h), fs.q1, __int2float_rn(l) * fs.q2);
 }
@@ -781,6 +771,44 @@ __device__ __forceinline__ void pull_voxel_lean(const LaunchArgs& a, int b, long
         o[0] = acc[0];
         o[n1] = acc[1];
         o[2 * n1] = acc[2];
+    }
+}
+
+// push_voxel_global (pp_voxel.cuh) for plain push, inlined with the z loop
+// rolled (weights and offsets rotate through slot 0) so that the fallback of the
+// batched kernel pins no registers across a call.
+template <int DP, typename IT>
+__device__ __forceinline__ void push_voxel_lean(const LaunchArgs& a, int b, long long v, float x0, float x1,
+                                                float x2) {
+    const Geometry& g = a.g;
+    const long long n1 = g.n1;
+    const IT sy = (IT)g.d0[0];
+    const IT sz = (IT)(g.d0[0] * g.d0[1]);
+#pragma unroll 1
+    for (int c = 0; c < g.nc; ++c) {
+        const float v0 = __ldg(a.in + ((long long)b * g.nc + c) * n1 + v);
+        if (!finitef(v0)) continue;
+        int b0, b1, b2;
+        bnd_code(a, c, b0, b1, b2);
+        Axis<DP, 0, IT> ax, ay, az;
+        ax.setup(x0, g.dp[0], b0, g.d0[0], (IT)1);
+        ay.setup(x1, g.dp[1], b1, g.d0[1], sy);
+        az.setup(x2, g.dp[2], b2, g.d0[2], sz);
+        float* f0 = a.out + ((long long)b * g.nc + c) * g.n0;
+#pragma unroll 1
+        for (int k = 0; k < DP; ++k) {
+#pragma unroll
+            for (int j = 0; j < DP; ++j) {
+                const float cb = v0 * (ay.w[j] * az.w[0]);
+#pragma unroll
+                for (int i = 0; i < DP; ++i) atomicAdd(f0 + (az.off[0] + ay.off[j] + ax.off[i]), cb * ax.w[i]);
+            }
+#pragma unroll
+            for (int i = 0; i + 1 < DP; ++i) {
+                az.w[i] = az.w[i + 1];
+                az.off[i] = az.off[i + 1];
+            }
+        }
     }
 }
 
@@ -1444,9 +1472,7 @@ __global__ void __launch_bounds__(kThreads, DP <= 3 ? 3 : 2) k_fused_tiled(const
                     const unsigned off = 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
                     const unsigned p = smem_addr(buf) + off;
                     float r[6];
-                    contract<kPullValGrad, DP>(wx, wy, wz, DP, DP, DP, false,
-                                               [&](int k, int jj, int i) { return lds_f32(p + k * Q4 + jj * P4 + 4u * i); },
-                                               r);
+                    contract_smem<kPullValGrad, DP>(wx, wy, wz, p, P4, Q4, r);
                     res = r[3] - gv;
                     grad[0] = r[0];
                     grad[1] = r[1];
@@ -1571,7 +1597,7 @@ __device__ __forceinline__ void batch_tile(const BatchItem& it, int lt, float* s
                 continue;
             }
             pull_voxel_lean<DP, kPull, int>(a, 0, iv[q], X[q][0], X[q][1], X[q][2]);
-            push_tile_fallback<DP, kPush, int>(pb, 0, iv[q], X[q][0], X[q][1], X[q][2]);
+            push_voxel_lean<DP, int>(pb, 0, iv[q], X[q][0], X[q][1], X[q][2]);
         }
         __syncthreads();   // box record reused by the next tile
         return;
@@ -1604,8 +1630,7 @@ __device__ __forceinline__ void batch_tile(const BatchItem& it, int lt, float* s
             const unsigned P4 = 4u * box.P, Q4 = 4u * box.Q;
             const unsigned p = smem_addr(fbox) + 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
             float r[6];
-            contract<kPull, DP>(wx, wy, wz, DP, DP, DP, false,
-                                [&](int k, int jj, int i) { return lds_f32(p + k * Q4 + jj * P4 + 4u * i); }, r);
+            contract_smem<kPull, DP>(wx, wy, wz, p, P4, Q4, r);
             f1[iv[q]] = r[0];
             val[q] = r[0];
             if (finitef(r[0])) bound += fabsf(r[0]);
