@@ -107,6 +107,25 @@ def test_fused_step_vs_oracle(pkg, O, path, deg, bnd, ext, nc):
     assert rel_err(L.to_numpy(dphi), ref_dphi) <= 1e-4
 
 
+def test_fused_step_batch_of_two(pkg, O, path):
+    """Two channels and a batch of two: the loss sums over both, df and dphi are
+    per batch element (the oracle runs each element on its own)."""
+    L = pkg.layout
+    rng = np.random.default_rng(47)
+    d0, d1 = (31, 27, 22), (29, 26, 20)
+    f0 = _f(rng, d0 + (2, 2))
+    phi = np.asfortranarray(np.stack([_phi(O, rng, d1, d0, 1.5) for _ in range(2)], axis=-1))
+    g = _f(rng, d1 + (2, 2))
+    s, so = pkg.Settings(3, (0, 1, 2), 1), O.Sett.make(3, (0, 1, 2), 1)
+    loss, df, dphi = pkg.fused_step(L.from_numpy(f0), L.from_numpy(phi), L.from_numpy(g), s)
+    parts = [_oracle_fused(O, np.asfortranarray(f0[..., b]), np.asfortranarray(phi[..., b]),
+                           np.asfortranarray(g[..., b]), so) for b in range(2)]
+    ref_loss = sum(p[0] for p in parts)
+    assert abs(float(loss) - ref_loss) <= 1e-5 * abs(ref_loss)
+    assert rel_err(L.to_numpy(df), np.stack([p[1] for p in parts], axis=-1)) <= 1e-4
+    assert rel_err(L.to_numpy(dphi), np.stack([p[2] for p in parts], axis=-1)) <= 1e-4
+
+
 def test_fused_step_nan_and_reproducible(pkg, O, path):
     """ext = 0 voxels outside the band make the loss NaN and their dphi NaN; the loss
     is bit-identical from run to run (fixed-order reduction)."""
