@@ -34,6 +34,15 @@ def test_library_exports_declared_symbols(pkg):
     assert lib.pp_version() >= 100
 
 
+def test_julia_binding_uses_declared_symbols():
+    """Every library symbol the Julia drop-in module calls is declared in the header
+    (the module itself needs Julia and CUDA.jl, which this suite does not run)."""
+    jl = open(os.path.join(ROOT, "pushpull.jl_gb300", "julia", "PushPullGB300.jl")).read()
+    used = set(re.findall(r"_sym\(:(\w+)\)", jl)) | set(re.findall(r":(pp_\w+)", jl))
+    assert {"pp_pull", "pp_push", "pp_fused_step", "pp_pull_grad_dot", "pp_last_error"} <= used
+    assert used <= set(_declared()), used - set(_declared())
+
+
 def _call_pull(lib, deg=(1, 1, 1), bnd=(1, 1, 1), nbnd=1, nc=1, nb=1, d0=(4, 4, 4), d1=(3, 3, 3),
                ptr=8):
     b = (C.c_int * len(bnd))(*bnd)
