@@ -44,6 +44,27 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def _errors(got, ref, floor=1e-3):
+    """FP64-oracle error of a result: norm-wise max|a-b| / max|b| and elementwise
+    max |a-b| / |b| over entries with |b| > floor * max|b| (NaN entries must agree)."""
+    a = np.asarray(got, np.float64).ravel(order="F")
+    b = np.asarray(ref, np.float64).ravel(order="F")
+    nan_ok = bool((np.isnan(a) == np.isnan(b)).all())
+    m = ~np.isnan(b)
+    a, b = a[m], b[m]
+    if b.size == 0:
+        return {"norm": 0.0, "elem": 0.0, "elem_floor": floor, "nan_masks_equal": nan_ok}
+    mx = float(np.abs(b).max())
+    big = np.abs(b) > floor * mx
+    norm = float(np.abs(a - b).max() / mx) if mx > 0 else float(np.abs(a).max())
+    elem = float((np.abs(a[big] - b[big]) / np.abs(b[big])).max()) if big.any() else 0.0
+    return {"norm": norm, "elem": elem, "elem_floor": floor, "nan_masks_equal": nan_ok}
+
+
+def _oracle_threads():
+    return max(1, min(32, os.cpu_count() or 1))
+
+
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each kernel
 # on this workload, from one ncu capture (profiles/k_pull_tiled_192cubic.md, profiles/k_push_tiled_192cubic.md).
 TRAFFIC = {"pull": 126_790_144, "push": 152_880_128}
@@ -239,6 +260,17 @@ def run_gpu(args):
         if i >= 3:
             pg_ms.append(e0.elapsed_time(e1))
     del g1
+    # FP64 error of the benchmarked pull and push (outside every timed region):
+    # f1 and acc hold the last timed step's outputs
+    accuracy = None
+    if not args.no_accuracy:
+        from oracle import oracle as O
+        so = O.Sett.make(w.deg, w.bnd, w.ext)
+        th = _oracle_threads()
+        f1n = L.to_numpy(f1)
+        accuracy = {"pull": _errors(f1n, O.pull(w.f0, w.phi, so, threads=th)),
+                    "push": _errors(L.to_numpy(acc), O.push(f1n, w.phi, d0, so, threads=th)),
+                    "reference": "FP64 oracle (oracle/pp_oracle.c) on the same inputs, whole volume"}
     pull_ms = [e[0].elapsed_time(e[1]) for e in evs]
     push_ms = [e[1].elapsed_time(e[2]) for e in evs]
     step_ms = statistics.mean(a + b for a, b in zip(pull_ms, push_ms))
@@ -327,6 +359,7 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded): smoothed U(0,1) image, smoothed "
             "random displacement", "config": _config(w, args), "roofline": roof, "cpu_baseline": cpu,
             "e2e": e2e, "gpu_launches": 2 * args.steps, "clocks": clk.summary(), "kernels": kernels,
+            "accuracy_vs_fp64": accuracy,
             "fused_step": fused, "batched": batched, "contention_push": contention,
             "wall_s_timed_region": wall}
     print(json.dumps(line), flush=True)
@@ -390,6 +423,19 @@ def fused_vs_plain(pkg, dev, args):
     def rel(a, b):
         a, b = a.double(), b.double()
         return float((a - b).abs().max() / b.abs().max())
+    accuracy = None
+    if not args.no_accuracy:
+        from oracle import oracle as O
+        so, th = O.Sett.make(w.deg, w.bnd, w.ext), _oracle_threads()
+        gn = L.to_numpy(g)
+        r = O.pull(w.f0, w.phi, so, threads=th) - gn
+        ref_loss = float(np.sum(r * r))
+        d = np.asfortranarray((2 * r).astype(np.float32))
+        accuracy = {"loss": abs(float(lf) - ref_loss) / abs(ref_loss),
+                    "df": _errors(L.to_numpy(dff), O.push(d, w.phi, d0, so, threads=th)),
+                    "dphi": _errors(L.to_numpy(dpf), O.pull_grad(w.f0, w.phi, so, threads=th) * (2 * r)[..., None],
+                                    floor=1e-2),
+                    "reference": "FP64 oracle on the same inputs, whole volume"}
     bytes_fused = 12 * n1 + 4 * int(np.prod(d0)) + 4 * n1 + 12 * n1 + 4 * int(np.prod(d0))
     return {"workload": "loss = sum((pull(f, phi) - g)^2), 160x192x160 Float32, degree 2, bounds (0,1,2), "
                         "ext=1, g = pull(f, phi2)",
@@ -399,7 +445,7 @@ def fused_vs_plain(pkg, dev, args):
             "rel_diff_fused_vs_plain": {"loss": abs(float(lf) - float(lp)) / abs(float(lp)),
                                         "df": rel(dff, dfp), "dphi": rel(dpf, dpp)},
             "plain": "pull, pull_grad, push kernels + torch residual/reduction/contraction (5 launches + 4 torch ops)",
-            "accuracy_vs_fp64": "checked in tests/test_gpu_full.py at this size (<= 1e-4 relative)"}
+            "accuracy_vs_fp64": accuracy}
 
 
 def _timeit(fn, reps, flush):
@@ -487,6 +533,16 @@ def contention_leg(pkg, dev, args):
     t_pushg = _timeit(lambda: pkg.push_grad(g1, phi, d, s, out=out, accumulate=False), reps, flush)
     n1, nc = int(np.prod(d)), 3
     taps = 64
+    accuracy = None
+    if not args.no_accuracy:
+        from oracle import oracle as O
+        so, th = O.Sett.make(3, 1, 1), _oracle_threads()
+        pn = L.to_numpy(phi)
+        accuracy = {"push": _errors(L.to_numpy(pkg.push(f1, phi, d, s)),
+                                    O.push(L.to_numpy(f1), pn, d, so, threads=th)),
+                    "push_grad": _errors(L.to_numpy(pkg.push_grad(g1, phi, d, s)),
+                                         O.push_grad(L.to_numpy(g1), pn, d, so, threads=th), floor=1e-2),
+                    "reference": "FP64 oracle on the same inputs, whole volume"}
     return {"workload": "push and push_grad, 256^3 x 3 channels Float32, cubic, DCT-II, ext=1, phi = 0.25x "
                         "contraction about the centre + FWHM-12 field +-3 vox (source occupies ~1/64 of the grid)",
             "push_ms": t_push, "push_grad_ms": t_pushg,
@@ -495,7 +551,7 @@ def contention_leg(pkg, dev, args):
                                       "push_grad": n1 * nc * taps / (t_pushg * 1e-3)},
             "note": "scatter updates = voxels x channels x 64 taps, accumulated in shared memory as fixed-point "
                     "integers (privatised) and flushed to HBM once per box word",
-            "accuracy_vs_fp64": "tests/test_gpu_full.py::test_c5_contention_push_vs_oracle"}
+            "accuracy_vs_fp64": accuracy}
 
 
 def main(argv=None):
@@ -511,6 +567,7 @@ def main(argv=None):
     ap.add_argument("--no-fused", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-contention", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 error fields")
     args = ap.parse_args(argv)
     import __graft_entry__ as entry
     entry.package()

@@ -10,7 +10,7 @@
  *    module-global __constant__ settings (ext/pushpull_gpu.jl:268-274, 380-383).
  *
  * 2. Compatibility layer: the exact symbols and signatures of the reference's
- *    CPU library (artifacts/C/pushpull.h:1-14, plus pullh at pushpull.c:111)
+ *    CPU library (artifacts/C/pushpull.h:1-14, plus pullh at pushpull.c:70)
  *    on HOST pointers, one (channel, batch) slice per call, so the reference's
  *    own ccall sites (src/pushpull_cpu.jl:45, 100, 140, 195, 251, 294, 337)
  *    bind to this library unchanged.  Each call copies its inputs to the
@@ -60,20 +60,20 @@ enum pp_status {
 /* ------------------------------------------------------------------------ */
 
 /* f1 = pull(f0, phi): replaces pull (src/pushpull_cpu.jl:17-53,
- * ext/pushpull_gpu.jl:15-51; per-voxel pull, artifacts/C/pushpull.c:55-74).
+ * ext/pushpull_gpu.jl:15-51; per-voxel pull, artifacts/C/pushpull.c:14-33).
  * Invalid voxels (non-finite phi, or outside the band when ext == 0) get NaN. */
 int pp_pull(float *f1, const float *phi, const float *f0,
             const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
             const int *bnd, int nbnd, const int deg[3], int ext, void *stream);
 
 /* g1 = pull_grad(f0, phi), 3 planar components per channel: replaces pull_grad
- * (src/pushpull_cpu.jl:69-108, ext/pushpull_gpu.jl:66-101; pullg, pushpull.c:78-107). */
+ * (src/pushpull_cpu.jl:69-108, ext/pushpull_gpu.jl:66-101; pullg, pushpull.c:37-66). */
 int pp_pull_grad(float *g1, const float *phi, const float *f0,
                  const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
                  const int *bnd, int nbnd, const int deg[3], int ext, void *stream);
 
 /* h1 = pull_hess(f0, phi), symmetric 3x3 (9 planar components) per channel:
- * replaces pull_hess (src/pushpull_cpu.jl:111-148; pullh, pushpull.c:111-143). */
+ * replaces pull_hess (src/pushpull_cpu.jl:111-148; pullh, pushpull.c:70-102). */
 int pp_pull_hess(float *h1, const float *phi, const float *f0,
                  const pp_usize d0[3], const pp_usize d1[3], int nc, int nb,
                  const int *bnd, int nbnd, const int deg[3], int ext, void *stream);
@@ -96,7 +96,7 @@ int pp_pull_hess_dot(float *dphi, const float *phi, const float *f0, const float
                      const int *bnd, int nbnd, const int deg[3], int ext, void *stream);
 
 /* f0 (+)= push(f1, phi): replaces push (src/pushpull_cpu.jl:165-203,
- * ext/pushpull_gpu.jl:165-201; push, pushpull.c:147-164).  accumulate != 0 adds
+ * ext/pushpull_gpu.jl:167-204; push, pushpull.c:106-123).  accumulate != 0 adds
  * into the caller's f0 (the reference contract: the caller zero-fills);
  * accumulate == 0 zeroes f0 on the stream first.  Non-finite f1 values and
  * invalid voxels are skipped. */
@@ -106,7 +106,7 @@ int pp_push(float *f0, const float *phi, const float *f1,
             int accumulate, void *stream);
 
 /* g0 (+)= push_grad(g1, phi), the adjoint of pull_grad: replaces push_grad
- * (src/pushpull_cpu.jl:220-259, ext/pushpull_gpu.jl:220-259; pushg_element,
+ * (src/pushpull_cpu.jl:220-259, ext/pushpull_gpu.jl:221-259; pushg_element,
  * artifacts/C/pushpull.cu:145-163).  Voxels with a non-finite gradient
  * component are skipped. */
 int pp_push_grad(float *g0, const float *phi, const float *g1,
@@ -250,6 +250,14 @@ const char *pp_last_error(void);
  * clears it.  Returns 0xffffffff if it cannot be read.  No reference
  * counterpart (the reference kernels never wait). */
 unsigned pp_device_status(int reset);
+
+/* Test of the timeout path of the bounded device-side waits: launches one warp
+ * that waits on a shared-memory barrier nothing will complete, giving up after
+ * limit_cycles SM clock cycles (1 .. 2^31, about a second at most).  The wait
+ * records bit 0 of the device status word and the kernel returns normally, so
+ * the context stays usable; read the bit with pp_device_status.  No reference
+ * counterpart (the reference kernels never wait). */
+int pp_test_bounded_wait(long long limit_cycles, void *stream);
 
 /* Library version: major*10000 + minor*100 + patch. */
 int pp_version(void);

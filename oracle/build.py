@@ -3,24 +3,35 @@
 * ``lib/libpp_oracle.so``  -- the FP64 oracle and FP32 port from ``pp_oracle.c``.
 * ``_ref/libpp_ref.so``    -- the reference's own CPU library, compiled from its
   C sources (``artifacts/C/pushpull.c``, which #includes ``pushpull_dev.cu``,
-  ``bspline.cu`` and ``patch.cu``) wherever the reference tree is present.  The
-  flags keep float contraction off so the build does what the source says.
+  ``bspline.cu`` and ``patch.cu``).  The flags keep float contraction off so the
+  build does what the source says.
 
-Nothing here is used by the shipped library.
+Where the reference tree is present (its location is ``$PP_REFERENCE_DIR``,
+default ``/root/reference``), ``stage_ref_sources`` copies those five files,
+unmodified, into ``_ref/src/``.  ``_ref/`` is kept out of version control but
+travels with the working copy, so a host without the reference tree (the GPU
+machine) compiles the same sources with its own compiler; no binary moves
+between hosts.  Nothing here is used by the shipped library.
 """
 from __future__ import annotations
 
 import os
+import shutil
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "lib", "libpp_oracle.so")
-REF_SO = os.path.join(HERE, "_ref", "libpp_ref.so")
-REF_SRC_DIR = "/root/reference/artifacts/C"
-REF_SRC = os.path.join(REF_SRC_DIR, "pushpull.c")
+REF_DIR = os.path.join(HERE, "_ref")
+REF_SO = os.path.join(REF_DIR, "libpp_ref.so")
+REF_STAGE = os.path.join(REF_DIR, "src")
 REF_DEPS = ("pushpull.c", "pushpull_dev.cu", "bspline.cu", "patch.cu", "cuheader.h")
 
 CC = os.environ.get("CC", "gcc")
+
+
+def reference_src_dir() -> str:
+    """The reference's ``artifacts/C`` directory (``$PP_REFERENCE_DIR``, default /root/reference)."""
+    return os.path.join(os.environ.get("PP_REFERENCE_DIR", "/root/reference"), "artifacts", "C")
 
 
 def _stale(target: str, sources) -> bool:
@@ -35,8 +46,9 @@ def oracle_cmd() -> list[str]:
             os.path.join(HERE, "pp_oracle.c"), "-lm"]
 
 
-def ref_cmd() -> list[str]:
-    return [CC, "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-o", REF_SO, REF_SRC, "-lm"]
+def ref_cmd(src_dir: str) -> list[str]:
+    return [CC, "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-o", REF_SO,
+            os.path.join(src_dir, "pushpull.c"), "-lm"]
 
 
 def build_oracle(force: bool = False) -> str:
@@ -48,17 +60,34 @@ def build_oracle(force: bool = False) -> str:
 
 
 def reference_present() -> bool:
-    return os.path.exists(REF_SRC)
+    return all(os.path.exists(os.path.join(reference_src_dir(), f)) for f in REF_DEPS)
+
+
+def stage_ref_sources() -> bool:
+    """Copy the reference's five C sources into ``_ref/src`` (when the tree is here)."""
+    if not reference_present():
+        return False
+    os.makedirs(REF_STAGE, exist_ok=True)
+    for f in REF_DEPS:
+        src, dst = os.path.join(reference_src_dir(), f), os.path.join(REF_STAGE, f)
+        if _stale(dst, [src]):
+            shutil.copyfile(src, dst)
+    return True
+
+
+def _staged() -> bool:
+    return all(os.path.exists(os.path.join(REF_STAGE, f)) for f in REF_DEPS)
 
 
 def build_ref(force: bool = False) -> str | None:
-    """Compile the reference CPU library from source; None when the tree is absent."""
-    if not reference_present():
-        return REF_SO if os.path.exists(REF_SO) else None
-    deps = [os.path.join(REF_SRC_DIR, f) for f in REF_DEPS]
+    """Compile the reference CPU library from its sources; None when neither the
+    reference tree nor a staged copy of its sources is available."""
+    stage_ref_sources()
+    if not _staged():
+        return None
+    deps = [os.path.join(REF_STAGE, f) for f in REF_DEPS]
     if force or _stale(REF_SO, deps):
-        os.makedirs(os.path.dirname(REF_SO), exist_ok=True)
-        subprocess.run(ref_cmd(), check=True)
+        subprocess.run(ref_cmd(REF_STAGE), check=True)
     return REF_SO
 
 

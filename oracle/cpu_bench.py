@@ -12,7 +12,7 @@ only where it could be built) or the FP32 port with the same signatures
   accumulator; the accumulators are then summed (timed).
 
 The reference library is single threaded (its OpenMP pragma is commented out,
-artifacts/C/pushpull.c:59-61); this harness only runs independent calls in
+artifacts/C/pushpull.c:18-20); this harness only runs independent calls in
 parallel, as a user would.
 """
 from __future__ import annotations

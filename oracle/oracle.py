@@ -37,7 +37,7 @@ _NAMES = {
                    pull_affine="ora_pull_affine", push_affine="ora_push_affine"),
     "port": dict(pull="port_pull", pullg="port_pullg", push="port_push",
                  pushg="port_pushg"),
-    # the reference's CPU pushg adds nothing for finite input (pushpull.c:185),
+    # the reference's CPU pushg adds nothing for finite input (pushpull.c:144),
     # so it is not exposed; push_grad parity uses the oracle and the adjoint.
     "ref": dict(pull="pull", pullg="pullg", pullh="pullh", push="push",
                 pull_affine="pull_affine", push_affine="push_affine"),
@@ -134,8 +134,10 @@ def _check_f(a):
     return np.asfortranarray(a)
 
 
-def pull(f0, phi, sett, kind: str = "oracle", _op: str = "pull"):
-    """f1 = pull(f0, phi) -- src/pushpull_cpu.jl:17-53 (pull_grad :69, pull_hess :111)."""
+def pull(f0, phi, sett, kind: str = "oracle", _op: str = "pull", threads: int = 1):
+    """f1 = pull(f0, phi) -- src/pushpull_cpu.jl:17-53 (pull_grad :69, pull_hess :111).
+
+    ``threads`` > 1 splits each (batch, channel) call into voxel slabs run in parallel."""
     sett = _as_sett(sett)
     f0, phi = _check_f(f0), _check_f(phi)
     assert 3 <= f0.ndim <= 5 and 4 <= phi.ndim <= 5 and phi.shape[3] == 3
@@ -160,21 +162,75 @@ def pull(f0, phi, sett, kind: str = "oracle", _op: str = "pull"):
         for c in range(nc):
             bnd = _i32(sett.bnd_for(c))
             o = of[ncomp * n1 * (nc * b + c):]
+            if threads > 1 and n1 >= 4 * threads:
+                _pull_slabs(fn, o, pf[3 * n1 * b:3 * n1 * (b + 1)], ff[n0 * (nc * b + c):], d0, n1, ncomp,
+                            bnd, dp, sett.ext, threads, out.dtype)
+                continue
             fn(_ptr(o), _ptr(pf[3 * n1 * b:]), _ptr(ff[n0 * (nc * b + c):]),
                d0, C.c_ulonglong(n1), bnd, dp, C.c_int(sett.ext))
     return out
 
 
-def pull_grad(f0, phi, sett, kind: str = "oracle"):
-    return pull(f0, phi, sett, kind, "pullg")
+def _slabs(n1, threads):
+    edges = np.linspace(0, n1, threads + 1).astype(np.int64)
+    return [(int(edges[t]), int(edges[t + 1])) for t in range(threads) if edges[t + 1] > edges[t]]
 
 
-def pull_hess(f0, phi, sett, kind: str = "oracle"):
-    return pull(f0, phi, sett, kind, "pullh")
+def _planar_slab(flat, n1, comps, a, b):
+    """Components [a, b) of a planar (n1, comps) array as a contiguous planar block."""
+    return np.ascontiguousarray(flat[:comps * n1].reshape(comps, n1)[:, a:b]).reshape(-1)
 
 
-def push(f1, phi, d0, sett, kind: str = "oracle", _op: str = "push"):
-    """f0 = push(f1, phi, d0) -- src/pushpull_cpu.jl:165-203 (push_grad :220-259)."""
+def _pull_slabs(fn, o, pf, ff, d0, n1, ncomp, bnd, dp, ext, threads, dtype):
+    """One (batch, channel) pull split into contiguous voxel slabs run on a thread
+    pool (the C calls release the GIL); each slab gets its own planar copy of its
+    deformation, as the reference ABI addresses component k at phi[i + k*n]"""
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(ab):
+        a, b = ab
+        n = b - a
+        ph = _planar_slab(pf, n1, 3, a, b)
+        res = np.zeros(ncomp * n, dtype=dtype)
+        fn(_ptr(res), _ptr(ph), _ptr(ff), d0, C.c_ulonglong(n), bnd, dp, C.c_int(ext))
+        o[:ncomp * n1].reshape(ncomp, n1)[:, a:b] = res.reshape(ncomp, n)
+
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(one, _slabs(n1, threads)))
+
+
+def _push_slabs(fn, o, pf, ff, dd, n0, n1, ncomp, bnd, dp, ext, threads, dtype):
+    """One (batch, channel) push split into voxel slabs, each scattering into a
+    private zeroed image; the private images are summed in slab order."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(ab):
+        a, b = ab
+        n = b - a
+        ph = _planar_slab(pf, n1, 3, a, b)
+        vals = _planar_slab(ff, n1, ncomp, a, b)
+        acc = np.zeros(n0, dtype=dtype)
+        fn(_ptr(acc), _ptr(ph), _ptr(vals), dd, C.c_ulonglong(n), bnd, dp, C.c_int(ext))
+        return acc
+
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        parts = list(ex.map(one, _slabs(n1, threads)))
+    for acc in parts:
+        o[:n0] += acc
+
+
+def pull_grad(f0, phi, sett, kind: str = "oracle", threads: int = 1):
+    return pull(f0, phi, sett, kind, "pullg", threads)
+
+
+def pull_hess(f0, phi, sett, kind: str = "oracle", threads: int = 1):
+    return pull(f0, phi, sett, kind, "pullh", threads)
+
+
+def push(f1, phi, d0, sett, kind: str = "oracle", _op: str = "push", threads: int = 1):
+    """f0 = push(f1, phi, d0) -- src/pushpull_cpu.jl:165-203 (push_grad :220-259).
+
+    ``threads`` > 1 splits each (batch, channel) call into voxel slabs run in parallel."""
     sett = _as_sett(sett)
     f1, phi = _check_f(f1), _check_f(phi)
     grad = _op == "pushg"
@@ -201,14 +257,19 @@ def push(f1, phi, d0, sett, kind: str = "oracle", _op: str = "push"):
     for b in range(nb):
         for c in range(nc):
             bnd = _i32(sett.bnd_for(c))
+            if threads > 1 and n1 >= 4 * threads:
+                _push_slabs(fn, of[n0 * (nc * b + c):n0 * (nc * b + c + 1)], pf[3 * n1 * b:3 * n1 * (b + 1)],
+                            ff[ncomp * n1 * (nc * b + c):], dd, n0, n1, ncomp, bnd, dp, sett.ext, threads,
+                            out.dtype)
+                continue
             fn(_ptr(of[n0 * (nc * b + c):]), _ptr(pf[3 * n1 * b:]),
                _ptr(ff[ncomp * n1 * (nc * b + c):]),
                dd, C.c_ulonglong(n1), bnd, dp, C.c_int(sett.ext))
     return out
 
 
-def push_grad(g1, phi, d0, sett, kind: str = "oracle"):
-    return push(g1, phi, d0, sett, kind, "pushg")
+def push_grad(g1, phi, d0, sett, kind: str = "oracle", threads: int = 1):
+    return push(g1, phi, d0, sett, kind, "pushg", threads)
 
 
 def adjust_affine(A):
@@ -221,7 +282,7 @@ def adjust_affine(A):
 
 
 def pull_affine(f0, A, d1, sett, kind: str = "oracle"):
-    """src/pushpull_cpu.jl:268-307 with the reference C at pushpull.c:217-250."""
+    """src/pushpull_cpu.jl:268-307 with the reference C at pushpull.c:176-209."""
     sett = _as_sett(sett)
     f0 = _check_f(f0)
     B = np.asfortranarray(adjust_affine(A))
@@ -242,7 +303,7 @@ def pull_affine(f0, A, d1, sett, kind: str = "oracle"):
 
 
 def push_affine(f1, A, d0, sett, kind: str = "oracle"):
-    """src/pushpull_cpu.jl:310-349 with the reference C at pushpull.c:254-285."""
+    """src/pushpull_cpu.jl:310-349 with the reference C at pushpull.c:213-244."""
     sett = _as_sett(sett)
     f1 = _check_f(f1)
     B = np.asfortranarray(adjust_affine(A))

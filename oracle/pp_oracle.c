@@ -13,13 +13,13 @@
  *   taps o_k .. o_k+dp_k-1, each mapped into [0, d0_k) by the boundary rule
  *   with a sign (patch.cu:5-59): 0 circulant, 1 mirror (DCT-II), 2 mirror with
  *   a sign flip on the mirrored half (DST-II); any other code acts as 1.
- *   pull  = sum w_i w_j w_k s f0[tap]     invalid -> NaN  (pushpull_dev.cu:236-245)
- *   pullg = gradient of that sum in voxel units, NaN x3   (pushpull_dev.cu:248-263)
- *   pullh = 3x3 Hessian, 9 planar comps, NaN x9           (pushpull.c:111-143)
+ *   pull  = sum w_i w_j w_k s f0[tap]     invalid -> NaN  (pushpull_dev.cu:61-70)
+ *   pullg = gradient of that sum in voxel units, NaN x3   (pushpull_dev.cu:73-88)
+ *   pullh = 3x3 Hessian, 9 planar comps, NaN x9           (pushpull.c:70-102)
  *   push  = adjoint of pull; skips non-finite values and invalid voxels
- *           (pushpull.c:147-164)
+ *           (pushpull.c:106-123)
  *   pushg = adjoint of pullg; skips invalid voxels and non-finite gradients.
- *           (The reference CPU pushg at pushpull.c:185 tests !ISFINITE(g[1]) and
+ *           (The reference CPU pushg at pushpull.c:144 tests !ISFINITE(g[1]) and
  *           so adds nothing for finite input; its GPU twin, pushpull.cu:145-163,
  *           adds every valid voxel.  The restatement follows the evident intent.)
  */
@@ -308,7 +308,7 @@ void ora_pushg(double *g0, const float *phi, const float *g1, const pp_usize *d0
 }
 
 /* affine position of output voxel (i,j,k), float ops in the reference order
- * (pushpull.c:231-241) */
+ * (pushpull.c:190-200) */
 static void affine_x(float x[3], const float *A, pp_usize i, pp_usize j, pp_usize k)
 {
     int c;

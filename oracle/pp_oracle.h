@@ -43,7 +43,7 @@ void ora_pushg(double *g0, const float *phi, const float *g1, const pp_usize *d0
 /* one-voxel pull at an arbitrary (float32) 1-based position, for finite differences */
 double ora_pull_at(const float pos[3], const float *f0, const pp_usize *d0,
                    const int *bnd, const pp_usize *dp, int ext);
-/* affine sampling: x = A(i,j,k) with A already shifted to 0-based (pushpull.c:217-285) */
+/* affine sampling: x = A(i,j,k) with A already shifted to 0-based (pushpull.c:176-244) */
 void ora_pull_affine(double *f1, const float *f0, const pp_usize *d0, pp_usize n1,
                      const pp_usize *d1, const float *A, const int *bnd,
                      const pp_usize *dp, int ext);

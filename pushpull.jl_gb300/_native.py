@@ -71,6 +71,7 @@ _SIGS = {
     "pp_set_path": (C.c_int, [C.c_int]),
     "pp_version": (C.c_int, []),
     "pp_device_status": (C.c_uint, [C.c_int]),
+    "pp_test_bounded_wait": (C.c_int, [C.c_longlong, _vp]),
     # compatibility layer: reference CPU signatures on host pointers
     "pull": (None, [_vp, _vp, _vp, _vp, C.c_ulonglong, _vp, _vp, C.c_int]),
     "pullg": (None, [_vp, _vp, _vp, _vp, C.c_ulonglong, _vp, _vp, C.c_int]),

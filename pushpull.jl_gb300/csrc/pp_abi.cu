@@ -94,6 +94,10 @@ TileCfg g_tiles[6][5];   // ops: pull, pull_grad, pull_hess, push, push_grad, fu
 bool g_tiles_init = false;
 int g_path = PP_PATH_AUTO;
 
+// The 8 x 8 x 16 tile (lx, ly, lz) = (3, 3, 4) selects the warp-specialised
+// pull kernels (pp_ws.cuh); every other shape the block-synchronous ones.
+bool is_ws_tile(const TileCfg& t) { return t.lx == 3 && t.ly == 3 && t.lz == 4 && t.cap > 0; }
+
 void init_tiles_locked() {
     if (g_tiles_init) return;
     // 8x8x8 tiles; the push family keeps two words per accumulator element; the
@@ -155,7 +159,7 @@ static int prepare(LaunchArgs& a, float* out, const float* phi, const float* in,
     if (!mul_ok(g.d0[0], g.d0[1], t) || !mul_ok(t, g.d0[2], g.n0)) return fail(PP_ERR_DIMS, "d0 overflows");
     if (!mul_ok(g.d1[0], g.d1[1], t) || !mul_ok(t, g.d1[2], g.n1)) return fail(PP_ERR_DIMS, "d1 overflows");
     for (int k = 0; k < 3; ++k) {
-        volatile float dk = (float)g.d0[k];   // float arithmetic, as artifacts/C/pushpull.c:8-10
+        volatile float dk = (float)g.d0[k];   // float arithmetic, as artifacts/C/pushpull.c:7-9
         g.hi[k] = dk - 0.99f;
     }
     g.nc = nc;
@@ -199,12 +203,22 @@ static int run_pull(int op, float* out, const float* phi, const float* f0, const
         if (!aligned4(up)) return fail(PP_ERR_ALIGN, "float pointers must be 4-byte aligned");
         a.up = up;
     }
-    const TileCfg t = tile_for(op < 3 ? op : op - 2, deg[0]);
-    cudaError_t e;
-    if (current_path() != PP_PATH_DIRECT && tiled_supported(a, t))
-        e = launch_pull_tiled(op, a, t, (cudaStream_t)stream);
-    else
-        e = launch_pull_direct(op, a, (cudaStream_t)stream);
+    TileCfg t = tile_for(op < 3 ? op : op - 2, deg[0]);
+    cudaError_t e = cudaErrorNotSupported;
+    const bool auto_path = current_path() != PP_PATH_DIRECT;
+    if (auto_path && is_ws_tile(t)) {
+        if (ws_supported(a)) e = launch_ws_pull(op, a, (cudaStream_t)stream);
+        if (e == cudaErrorNotSupported) {
+            (void)cudaGetLastError();
+            t = TileCfg{3, 3, 3, 8192};   // ops or geometries the warp-specialised kernels do not take
+        }
+    }
+    if (e == cudaErrorNotSupported) {
+        if (auto_path && t.cap > 0 && tiled_supported(a, t))
+            e = launch_pull_tiled(op, a, t, (cudaStream_t)stream);
+        else
+            e = launch_pull_direct(op, a, (cudaStream_t)stream);
+    }
     if (e != cudaSuccess) return cuda_fail(e, "pull launch");
     return PP_OK;
 }
@@ -364,8 +378,12 @@ int pp_set_tile(int op, int deg, int lx, int ly, int lz, int cap_floats) {
     pp::g_err.clear();
     if (op < -1 || op > 5) return pp::fail(PP_ERR_UNSUPPORTED, "op %d outside -1..5", op);
     if (deg < -1 || deg > 4) return pp::fail(PP_ERR_DEGREE, "deg %d outside -1..4", deg);
-    if (lx < 0 || ly < 0 || lz < 0 || lx + ly + lz < 5 || lx + ly + lz > 9)
-        return pp::fail(PP_ERR_UNSUPPORTED, "tile 2^%d x 2^%d x 2^%d must hold 32..512 voxels", lx, ly, lz);
+    const bool ws = lx == 3 && ly == 3 && lz == 4;   // the warp-specialised pull tile
+    if (!ws && (lx < 0 || ly < 0 || lz < 0 || lx + ly + lz < 5 || lx + ly + lz > 9))
+        return pp::fail(PP_ERR_UNSUPPORTED, "tile 2^%d x 2^%d x 2^%d must hold 32..512 voxels (or be 8x8x16)", lx,
+                        ly, lz);
+    if (ws && cap_floats != 0 && (op < 0 || op > 2))
+        return pp::fail(PP_ERR_UNSUPPORTED, "the 8x8x16 tile serves the pull family only");
     if (cap_floats != 0 && (cap_floats < 64 || (cap_floats & 3) || cap_floats > (227 * 1024) / 4))
         return pp::fail(PP_ERR_UNSUPPORTED, "cap %d floats must be 0 or a multiple of 4 in [64, 58112]",
                         cap_floats);
@@ -416,7 +434,7 @@ int pp_autotune(int op, float* out, const float* phi, const float* in, const pp_
             default: return pp_push_grad(out, phi, in, d0, d1, nc, nb, bnd, nbnd, deg, ext, 0, stream);
         }
     };
-    const int tiles[][3] = {{3, 3, 3}, {4, 3, 2}, {4, 2, 3}, {5, 2, 2}, {3, 4, 2}, {3, 3, 2}, {4, 2, 2}};
+    const int tiles[][3] = {{3, 3, 3}, {4, 3, 2}, {4, 2, 3}, {5, 2, 2}, {3, 4, 2}, {3, 3, 2}, {4, 2, 2}, {3, 3, 4}};
     const int caps_pull[] = {6144, 8192, 12288};
     const int caps_push[] = {12288, 16384, 20480};
     const TileCfg saved = tile_for(op, deg[0]);
@@ -453,8 +471,10 @@ int pp_autotune(int op, float* out, const float* phi, const float* in, const pp_
     }
     pp_set_path(PP_PATH_AUTO);
     for (const auto& t : tiles) {
-        for (int ci = 0; ci < 3 && rc == PP_OK; ++ci) {
-            const int cap = is_push ? caps_push[ci] : caps_pull[ci];
+        const bool ws = t[0] == 3 && t[1] == 3 && t[2] == 4;
+        if (ws && is_push) continue;
+        for (int ci = 0; ci < (ws ? 1 : 3) && rc == PP_OK; ++ci) {
+            const int cap = ws ? 9216 : (is_push ? caps_push[ci] : caps_pull[ci]);
             if (pp_set_tile(op, deg[0], t[0], t[1], t[2], cap) != PP_OK) continue;
             if ((rc = measure(ms)) != PP_OK) break;
             if (ms < bestv) {
@@ -490,6 +510,14 @@ int pp_autotune(int op, float* out, const float* phi, const float* in, const pp_
 }
 
 unsigned pp_device_status(int reset) { return pp::read_device_status(reset != 0); }
+
+int pp_test_bounded_wait(long long limit_cycles, void* stream) {
+    pp::g_err.clear();
+    if (limit_cycles < 1 || limit_cycles > (1LL << 31))
+        return pp::fail(PP_ERR_UNSUPPORTED, "limit_cycles %lld outside [1, 2^31]", limit_cycles);
+    const cudaError_t e = pp::launch_bounded_wait_probe(limit_cycles, (cudaStream_t)stream);
+    return e == cudaSuccess ? PP_OK : pp::cuda_fail(e, "bounded-wait probe launch");
+}
 
 }  // extern "C"
 

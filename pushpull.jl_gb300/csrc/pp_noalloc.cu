@@ -10,6 +10,9 @@
 // in a fixed array compiled into the library instead, so it calls no allocator.
 #include <mutex>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "pp_kernels.cuh"
 #include "pp_tiled.cuh"
 #include "pushpull_gb300.h"
@@ -34,24 +37,55 @@ static_assert(kPartialBytes % 256 == 0, "plane maxima must start 256-byte aligne
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 // In host code g_noalloc_scratch names a host-side shadow, not device memory:
-// the device address comes from cudaGetSymbolAddress, once per device, with that
-// device current.
+// the device address comes from cudaGetSymbolAddress, once per device and
+// context, with that device current.  The address is cached together with the
+// unique id of the context it was taken in; a call under a different context
+// (after cudaDeviceReset re-created the primary context, which reloads this
+// module) queries it again instead of using a stale address.
 constexpr int kMaxDevices = 64;
 std::mutex g_addr_mu;
 void* g_addr[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxDevices] = {};
+
+// Unique id of the current context (0 when the driver cannot say).
+unsigned long long current_context_id() {
+    static std::once_flag once;
+    static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+    static PFN_cuCtxGetId_v12000 get_id = nullptr;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(p);
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
 
 int scratch_address(void** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return pp::fail_status(PP_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return pp::fail_status(PP_ERR_UNSUPPORTED, "device %d out of range", dev);
+    // the runtime makes the device's primary context current with cudaGetSymbolAddress
+    // below on a first call; query the id after that, and compare on later calls
     std::lock_guard<std::mutex> lk(g_addr_mu);
-    if (!g_addr[dev]) {
+    const unsigned long long ctx = g_addr[dev] ? current_context_id() : 0;
+    if (!g_addr[dev] || ctx == 0 || ctx != g_ctx_id[dev]) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
             return pp::fail_status(PP_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
         g_addr[dev] = p;
+        g_ctx_id[dev] = current_context_id();
     }
     *out = g_addr[dev];
     return PP_OK;

@@ -17,6 +17,7 @@ unsigned status_push(bool reset);
 unsigned status_push_grad(bool reset);
 unsigned status_fused(bool reset);
 unsigned status_batch(bool reset);
+unsigned status_ws_pull(bool reset);
 
 bool tiled_supported(const LaunchArgs& a, const TileCfg& t) {
     const Geometry& g = a.g;
@@ -65,6 +66,29 @@ int fused_tiled_grid(const LaunchArgs& a, const TileCfg& c) {
 
 TileGrid tile_grid(const LaunchArgs& a, const TileCfg& c) { return make_grid(a, c); }
 
+namespace {
+// One warp waits on an mbarrier that no copy or thread will ever complete, with
+// a caller-given cycle limit: the bounded wait gives up, records the timeout in
+// this unit's status word and the kernel returns normally.
+__global__ void k_bounded_wait_probe(long long limit) {
+    __shared__ __align__(8) unsigned long long bar;
+    const unsigned a = smem_addr(&bar);
+    if (threadIdx.x == 0) {
+        mbar_init(a, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    mbar_wait_limit(a, 0u, limit);
+    __syncwarp();
+    if (threadIdx.x == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(a) : "memory");
+}
+}  // namespace
+
+cudaError_t launch_bounded_wait_probe(long long limit_cycles, cudaStream_t s) {
+    k_bounded_wait_probe<<<1, 32, 0, s>>>(limit_cycles);
+    return cudaGetLastError();
+}
+
 unsigned read_device_status(bool reset) {
     unsigned v = status_pull_basic(reset);
     v |= status_pull_hess(reset);
@@ -73,6 +97,8 @@ unsigned read_device_status(bool reset) {
     v |= status_push_grad(reset);
     v |= status_fused(reset);
     v |= status_batch(reset);
+    v |= status_ws_pull(reset);
+    v |= unit_status(reset);   // the bounded-wait probe of this unit
     return v;
 }
 

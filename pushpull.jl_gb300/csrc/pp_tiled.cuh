@@ -13,6 +13,10 @@ struct TileCfg {
 };
 
 bool tiled_supported(const LaunchArgs& a, const TileCfg& t);
+// warp-specialised pull family (8 x 8 x 16 tiles, pp_ws.cuh): geometry test and
+// launch (cudaErrorNotSupported for ops or layouts it does not take)
+bool ws_supported(const LaunchArgs& a);
+cudaError_t launch_ws_pull(int op, const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_pull_tiled(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s);
 cudaError_t launch_push_tiled(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s);
 
@@ -49,6 +53,10 @@ TileGrid tile_grid(const LaunchArgs& a, const TileCfg& c);
 // items in device memory; `counter` a zeroed device word for the work queue
 cudaError_t launch_batch(const BatchItem* items, int nitems, int total_tiles, unsigned* counter, int cap,
                          cudaStream_t s);
+
+// One warp, one CTA: a bounded wait on an mbarrier that never completes, with
+// the given cycle limit (test of the timeout path; records the timeout bit).
+cudaError_t launch_bounded_wait_probe(long long limit_cycles, cudaStream_t s);
 
 // Read (and optionally clear) the device status word of the current device:
 // bit 0 = a bounded device-side wait gave up.  0xffffffff if it cannot be read.

@@ -35,7 +35,7 @@
 //
 // Reference kernels replaced: pull_element / pullg_element / pullh_element /
 // push_element / pushg_element (artifacts/C/pushpull.cu:33-163); per-voxel math
-// pull1 / pullg1 / pullh1 / push1 / pushg1 (artifacts/C/pushpull_dev.cu:236-354).
+// pull1 / pullg1 / pullh1 / push1 / pushg1 (artifacts/C/pushpull_dev.cu:61-179).
 #include <climits>
 #include <cstring>
 #include <map>
@@ -505,19 +505,25 @@ __device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait: gives up after kWaitCycles clock cycles, records the failure
-// in the device status word and returns false.
+// Bounded wait: gives up after `limit` clock cycles, records the failure in
+// the device status word and returns false.  A kernel whose wait gave up skips
+// its remaining work and returns; copies it had already issued may still land
+// in its shared memory, so after a recorded timeout the context is suspect and
+// the caller should treat its outputs as undefined.
 constexpr long long kWaitCycles = 4000000000LL;   // about two seconds
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+__device__ __forceinline__ bool mbar_wait_limit(unsigned bar, unsigned parity, long long limit) {
     if (mbar_try(bar, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try(bar, parity)) {
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > limit) {
             atomicOr(&g_device_status, kStatusWaitTimeout);
             return false;
         }
     }
     return true;
+}
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+    return mbar_wait_limit(bar, parity, kWaitCycles);
 }
 __device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap* map, unsigned bar, int x, int y, int z,
                                             int w) {

@@ -83,7 +83,7 @@ __device__ __forceinline__ void pull_store(float* o, long long n1, const float (
         o[n1] = r[1];
         o[2 * n1] = r[2];
     } else {
-        // column-major 3x3, entry (p,q) at component p + 3q (artifacts/C/pushpull.c:129-134)
+        // column-major 3x3, entry (p,q) at component p + 3q (artifacts/C/pushpull.c:88-93)
         o[0] = r[0];
         o[4 * n1] = r[1];
         o[8 * n1] = r[2];

@@ -1,0 +1,45 @@
+// pp_ws_pull.cu -- warp-specialised pull and pull_grad kernels (pp_ws.cuh).
+#include "pp_ws.cuh"
+
+namespace pp {
+
+namespace {
+template <int OP, typename IT>
+cudaError_t ws_dispatch(const LaunchArgs& a, const TileGrid& t, const CUtensorMap& phimap, cudaStream_t s) {
+    switch (a.g.dp[0]) {
+        case 1: return launch_ws_one<1, OP, IT>(a, t, phimap, s);
+        case 2: return launch_ws_one<2, OP, IT>(a, t, phimap, s);
+        case 3: return launch_ws_one<3, OP, IT>(a, t, phimap, s);
+        case 4: return launch_ws_one<4, OP, IT>(a, t, phimap, s);
+        default: return launch_ws_one<5, OP, IT>(a, t, phimap, s);
+    }
+}
+}  // namespace
+
+bool ws_supported(const LaunchArgs& a) {
+    const Geometry& g = a.g;
+    if (!(g.dp[0] == g.dp[1] && g.dp[1] == g.dp[2])) return false;
+    // most of a tile inside the sample grid (degenerate grids go per voxel)
+    if (2 * g.d1[0] < 8 || 2 * g.d1[1] < 8 || 2 * g.d1[2] < 16) return false;
+    const long long ntx = (g.d1[0] + 7) >> 3, nty = (g.d1[1] + 7) >> 3, ntz = (g.d1[2] + 15) >> 4;
+    return ntx * nty * ntz * g.nb < 0x7fffffffLL;
+}
+
+// Warp-specialised pull family; cudaErrorNotSupported when the deformation
+// cannot be streamed by TMA (unaligned base or x extent), so the caller can
+// fall back to the other kernels.
+cudaError_t launch_ws_pull(int op, const LaunchArgs& a, cudaStream_t s) {
+    const TileGrid t = make_grid(a, TileCfg{kWsLx, kWsLy, kWsLz, kWsCap});
+    CUtensorMap phimap;
+    std::memset(&phimap, 0, sizeof phimap);
+    if (!encode_tile_map(&phimap, a.phi, a.g.d1, 3LL * a.g.nb, t, 3)) return cudaErrorNotSupported;
+    const bool small = a.g.n0 < (1LL << 31) - 1 && a.g.n1 < (1LL << 31) - 1;
+    if (op == kPull) return small ? ws_dispatch<kPull, int>(a, t, phimap, s) : ws_dispatch<kPull, long long>(a, t, phimap, s);
+    if (op == kPullGrad)
+        return small ? ws_dispatch<kPullGrad, int>(a, t, phimap, s) : ws_dispatch<kPullGrad, long long>(a, t, phimap, s);
+    return cudaErrorNotSupported;
+}
+
+unsigned status_ws_pull(bool reset) { return unit_status(reset); }
+
+}  // namespace pp

@@ -62,7 +62,7 @@ class Settings:
         return (C.c_int * len(self._packed))(*self._packed)
 
     def for_channel(self, c: int) -> "Settings":
-        """Settings of one channel (``sett_chan``, src/pushpull_general.jl:426-432)."""
+        """Settings of one channel (``sett_chan``, src/pushpull_general.jl:63-69)."""
         b = self.bnd[0] if len(self.bnd) == 1 else self.bnd[c]
         return Settings(self.deg, b, self.ext)
 

@@ -68,3 +68,27 @@ def rel_err(a, b) -> float:
 def golden_sett(O, case):
     bnd = [tuple(b) for b in case["bnd"]]
     return O.Sett.make(tuple(case["deg"]), bnd if len(bnd) > 1 else bnd[0], case["ext"])
+
+
+def elem_rel_err(a, b, floor: float = 1e-3) -> float:
+    """Elementwise relative error: max |a-b| / |b| over entries with
+    |b| > floor * max|b| (NaN masks must agree).  Entries below the floor are
+    left to the norm-wise ``rel_err``: a float32 sum whose terms cancel to near
+    zero carries an absolute, not a relative, rounding error."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    assert (np.isnan(a) == np.isnan(b)).all(), "NaN masks differ"
+    m = ~np.isnan(b)
+    if not m.any():
+        return 0.0
+    av, bv = a[m], b[m]
+    big = np.abs(bv) > floor * np.abs(bv).max()
+    if not big.any():
+        return 0.0
+    return float((np.abs(av[big] - bv[big]) / np.abs(bv[big])).max())
+
+
+def errors(a, b, floor: float = 1e-3) -> dict:
+    """Norm-wise and elementwise relative errors of ``a`` against ``b``."""
+    return {"norm": rel_err(a, b), "elem": elem_rel_err(a, b, floor)}

@@ -6,7 +6,7 @@ and records its outputs on seeded Float32 inputs:
 
 * ``pull``, ``pullg``, ``pullh``, ``push`` straight from the reference symbols;
 * ``pushg`` (push_grad) as the exact transpose of the reference ``pullg``: the
-  reference CPU ``pushg`` adds nothing for finite input (artifacts/C/pushpull.c:185),
+  reference CPU ``pushg`` adds nothing for finite input (artifacts/C/pushpull.c:144),
   so its golden values are built column by column from ``pullg`` applied to unit
   volumes and contracted with the input gradient field in float64;
 * ``pull_affine`` / ``push_affine`` from the reference affine symbols.
@@ -185,7 +185,7 @@ def main():
         for bnd in (0, 1, 2):
             add(f"far_d{deg}_b{bnd}", deg, bnd, 1, f0, phi, f1, g1)
 
-    # 8. affine pull / push (artifacts/C/pushpull.c:217-285)
+    # 8. affine pull / push (artifacts/C/pushpull.c:176-244)
     aff_cases = []
     for deg, bnd, ext in ((1, 1, 1), (3, 0, 1), (2, 2, 0), (0, 1, 0)):
         A = np.array([[0.9, 0.1, -0.05, 0.7], [-0.08, 1.1, 0.03, -0.4], [0.02, -0.06, 0.95, 0.3]],

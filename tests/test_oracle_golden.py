@@ -83,7 +83,7 @@ def test_oracle_affine_matches_reference(golden, O):
 
 
 def test_reference_cpu_pushg_defect_is_not_the_contract(O):
-    """The reference CPU pushg adds nothing for finite input (artifacts/C/pushpull.c:185);
+    """The reference CPU pushg adds nothing for finite input (artifacts/C/pushpull.c:144);
     the oracle's push_grad is the true adjoint of pull_grad instead."""
     if not O.ref_available():
         pytest.skip("reference sources not present")

@@ -35,29 +35,37 @@ def _run(lib, name, f0, phi, g, sett, nc, nb):
     return rc, loss, df, dphi
 
 
-def _inputs(pkg, O, seed, d0, d1, nc, scale):
+def _inputs(pkg, O, seed, d0, d1, nc, scale, nb=1):
     L = pkg.layout
     rng = np.random.default_rng(seed)
-    f0 = scale * rng.standard_normal(d0 + ((nc,) if nc > 1 else ())).astype(np.float32)
-    phi = O.identity(d1).astype(np.float64)
-    for k in range(3):
-        phi[..., k] = 1 + (phi[..., k] - 1) * (d0[k] - 1) / max(d1[k] - 1, 1)
-    phi = (phi + 1.5 * rng.standard_normal(phi.shape)).astype(np.float32)
-    g = scale * rng.standard_normal(d1 + ((nc,) if nc > 1 else ())).astype(np.float32)
+    cb = ((nc,) if nc > 1 or nb > 1 else ()) + ((nb,) if nb > 1 else ())
+    f0 = scale * rng.standard_normal(d0 + cb).astype(np.float32)
+    phis = []
+    for _ in range(nb):
+        phi = O.identity(d1).astype(np.float64)
+        for k in range(3):
+            phi[..., k] = 1 + (phi[..., k] - 1) * (d0[k] - 1) / max(d1[k] - 1, 1)
+        phis.append((phi + 1.5 * rng.standard_normal(phi.shape)).astype(np.float32))
+    phi = np.stack(phis, axis=-1) if nb > 1 else phis[0]
+    g = scale * rng.standard_normal(d1 + cb).astype(np.float32)
     return tuple(L.from_numpy(np.asfortranarray(a)) for a in (f0, phi, g))
 
 
 @pytest.mark.parametrize("path", [0, 1])
-def test_noalloc_matches_fused_step_two_calls(pkg, O, path):
+@pytest.mark.parametrize("nb", [1, 2])
+def test_noalloc_matches_fused_step_two_calls(pkg, O, path, nb):
+    """Two calls in a row (the second with different inputs); with nb = 2 the
+    per-(channel, batch) plane maxima and the per-batch loss partials are
+    compared for values as well."""
     lib = pkg.native_library()
     assert lib.pp_set_path(path) == 0
     try:
         sett = pkg.Settings(2, (0, 1, 2), 1)
         for call, (seed, scale) in enumerate([(1, 100.0), (2, 1.0)]):
-            f0, phi, g = _inputs(pkg, O, seed, (40, 36, 30), (38, 34, 28), 2, scale)
-            rc, loss, df, dphi = _run(lib, "pp_fused_step_noalloc", f0, phi, g, sett, 2, 1)
+            f0, phi, g = _inputs(pkg, O, seed + 10 * nb, (40, 36, 30), (38, 34, 28), 2, scale, nb)
+            rc, loss, df, dphi = _run(lib, "pp_fused_step_noalloc", f0, phi, g, sett, 2, nb)
             assert rc == 0, lib.pp_last_error()
-            rc, rloss, rdf, rdphi = _run(lib, "pp_fused_step", f0, phi, g, sett, 2, 1)
+            rc, rloss, rdf, rdphi = _run(lib, "pp_fused_step", f0, phi, g, sett, 2, nb)
             assert rc == 0, lib.pp_last_error()
             torch.cuda.synchronize()
             a, b = float(loss), float(rloss)
