@@ -120,7 +120,12 @@ typedef struct {
  *   beta_n'  = beta_{n-1}(u+1/2) - beta_{n-1}(u-1/2)
  *   beta_n'' = beta_{n-2}(u+1) - 2 beta_{n-2}(u) + beta_{n-2}(u-1)
  * degree 0 has zero derivatives and degree 1 a zero second derivative, as in
- * the reference (bspline.cu:154-156, 220-226). */
+ * the reference (bspline.cu:154-156, 220-226).  Degree 1 (first derivative)
+ * and degree 2 (second derivative) have piecewise-constant derivatives; for
+ * them the reference's constants are used at every t, (-1, 1)
+ * (bspline.cu:150-153) and (1, -2, 1) (bspline.cu:227-232), because the
+ * identity would be evaluated on a knot of the lower-degree spline when float
+ * rounding of a very large coordinate puts t on a knot (t = 0 for degree 1). */
 static void axis64_setup(axis64 *a, int dp, float x, int bnd, pp_usize d)
 {
     int k, n = dp - 1, sgn;
@@ -131,8 +136,11 @@ static void axis64_setup(axis64 *a, int dp, float x, int bnd, pp_usize d)
     for (k = 0; k < dp; ++k) {
         double u = t - (double)k;
         a->w[k]  = (n == 0) ? 1.0 : bspline(n, u);
-        a->dw[k] = (n == 0) ? 0.0 : bspline(n - 1, u + 0.5) - bspline(n - 1, u - 0.5);
+        a->dw[k] = (n == 0) ? 0.0
+                 : (n == 1) ? (k == 0 ? -1.0 : 1.0)
+                 : bspline(n - 1, u + 0.5) - bspline(n - 1, u - 0.5);
         a->hw[k] = (n <= 1) ? 0.0
+                 : (n == 2) ? (k == 1 ? -2.0 : 1.0)
                  : bspline(n - 2, u + 1.0) - 2.0 * bspline(n - 2, u) + bspline(n - 2, u - 1.0);
         a->idx[k] = fold_index(bnd, a->o + k, d, &sgn);
         a->sg[k]  = (double)sgn;

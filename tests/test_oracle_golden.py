@@ -100,3 +100,25 @@ def test_reference_cpu_pushg_defect_is_not_the_contract(O):
              (C.c_ulonglong * 3)(3, 3, 3), C.c_int(1))
     assert not out.any()
     assert np.abs(O.push_grad(g1, phi, d0, O.Sett.make(2, 1, 1))).max() > 0
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3, 4])
+def test_oracle_matches_reference_at_far_coordinates(O, deg):
+    """Coordinates of 1e9 (float32 spacing 64): float rounding puts the spline
+    offset t on a knot (t = 0 for degree 1), where the derivative weights of
+    degree 1 and the second-derivative weights of degree 2 are the reference's
+    constants.  The oracle must still agree with the reference library there."""
+    if not O.ref_available():
+        pytest.skip("reference sources not present")
+    rng = np.random.default_rng(400 + deg)
+    d = (12, 10, 9)
+    f0 = np.asfortranarray(rng.standard_normal(d + (2,)).astype(np.float32))
+    phi = (O.identity(d) + 2.0 * rng.standard_normal(d + (3,))).astype(np.float32)
+    flat = phi.reshape(-1, order="F")
+    flat[rng.choice(flat.size, 60, replace=False)] = 1e9
+    phi = np.asfortranarray(phi)
+    s = O.Sett.make(deg, 1, 1)
+    for op in ("pull", "pull_grad", "pull_hess"):
+        a = getattr(O, op)(f0, phi, s)
+        b = getattr(O, op)(f0, phi, s, kind="ref")
+        assert rel_err(a, b) <= TOL, (deg, op)
