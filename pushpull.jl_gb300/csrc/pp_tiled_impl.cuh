@@ -135,9 +135,10 @@ struct Box {
     int P, Q, size; // row pitch (P % 32 == pmod, P % 4 == 0), plane pitch (multiple of 32), floats
     int mode;       // 0 no valid voxel, 1 shared memory, 2 per-voxel global fallback
     int interior;   // bit k: the box lies inside the image along dimension k (no folding)
-    int tma;        // 1: the box is the fixed kTmaBox* window loaded by one TMA copy
+    int tma;        // 1: the box is a fixed window loaded by one TMA copy; 2: the same, with mirrored margins to complete
     float S;        // block sum of the caller's per-thread value (push: bound on sum |contribution|)
     int E;          // scale exponent of the fixed-point accumulator for S (see scale_exponent)
+    int wsc;        // push: 1 = scatter one voxel per warp instruction (contracted tile)
 };
 
 __device__ __forceinline__ int clamp_tap(long long o) {
@@ -160,12 +161,52 @@ __device__ __forceinline__ int scale_exponent(float S) {
     return (E < -80 || E > 100) ? INT_MIN : E;
 }
 
+// ---- pitches for the warp-cooperative scatter -------------------------------
+// One voxel per warp instruction, one tap per lane: lane l of pass p takes tap
+// t = 32 p + l, (i, j, k) = t in radix DP, at box element base + i + P j + Q k.
+// The taps of one voxel never share an element, and for (P mod 32, Q mod 32)
+// pairs whose bit is set below (bit Q of entry P, one row per DP = 3, 4, 5) the
+// 32 lanes of every pass also fall in 32 distinct shared-memory banks, so each
+// reduction is a single wavefront whatever the deformation does.
+__device__ const unsigned kScatterQMask[3][32] = {
+    {0x00000000u, 0x00000000u, 0x00000000u, 0x00e00e00u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00200800u,
+     0x00000000u, 0x20000008u, 0x20000008u, 0x22044088u, 0x00000000u, 0x00000000u, 0x00200800u, 0x00000000u,
+     0x00000000u, 0x00000000u, 0x00200800u, 0x00000000u, 0x00000000u, 0x22044088u, 0x20000008u, 0x20000008u,
+     0x00000000u, 0x00200800u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00e00e00u, 0x00000000u, 0x00000000u},
+    {0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00010000u, 0x00000000u, 0x00000000u, 0x00000000u,
+     0x10101010u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00010000u, 0x00000000u, 0x00000000u, 0x00000000u,
+     0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00010000u, 0x00000000u, 0x00000000u, 0x00000000u,
+     0x10101010u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00010000u, 0x00000000u, 0x00000000u, 0x00000000u},
+    {0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x02000000u, 0x00000000u, 0x00000000u,
+     0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u,
+     0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u,
+     0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u, 0x00000000u},
+};
+
+// Smallest row pitch P >= the row's 4-element groups (the flush reads whole
+// groups of 4) and plane pitch Q >= P * e1 of a conflict-free pair.
+template <int DP>
+__device__ __forceinline__ void scatter_pitch(long long e0, long long e1, long long& P, long long& Q) {
+    const unsigned* mask = kScatterQMask[DP - 3];
+    P = (e0 + 3) & ~3LL;
+    while (mask[P & 31] == 0u) ++P;
+    const unsigned m = mask[P & 31];
+    Q = P * e1;
+    while (!((m >> (Q & 31)) & 1u)) ++Q;
+}
+
 // Block-wide reduction of the first-tap bounds into the footprint box.
 // `words` = shared-memory words needed per box element (1 for pull, 2 for push).
 // Also sums `ssum` over the block into box.S (fixed order) and sets box.E.
-template <int DP>
+// WSCATTER (push): a tile whose box has fewer elements than the tile has
+// voxels (a contracting deformation, many voxels per element) gets the
+// warp-cooperative scatter when its accumulator and the voxel records
+// (rec_floats, kept at the top of the budget) fit: box.wsc = 1 and the
+// conflict-free pitches of scatter_pitch.
+template <int DP, bool WSCATTER = false>
 __device__ __forceinline__ void reduce_box(int (&mn)[3], int (&mx)[3], const TileGrid& t, const Geometry& g,
-                                           int words, Box& box, int (&red)[8][7], float ssum = 0.f) {
+                                           int words, Box& box, int (&red)[8][7], float ssum = 0.f,
+                                           int nv_tile = 0, int rec_floats = 0) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -202,6 +243,7 @@ __device__ __forceinline__ void reduce_box(int (&mn)[3], int (&mx)[3], const Til
         if (lo[0] > hi[0]) {
             box.mode = 0;
             box.tma = 0;
+            box.wsc = 0;
         } else {
             const int xo = lo[0] & ~3;
             long long e[3];
@@ -214,13 +256,23 @@ __device__ __forceinline__ void reduce_box(int (&mn)[3], int (&mx)[3], const Til
             if (lo[2] >= 0 && (long long)hi[2] + DP <= g.d0[2]) interior |= 4;
             // P % 32 == pmod and Q % 32 == 0 keep the warp's rows and planes in
             // disjoint banks; when that padding would not fit, pack tightly.
-            long long P = (e[0] + 3) & ~3LL;
-            long long Pp = P + (((t.pmod - (int)(P & 31)) + 32) & 31);
-            long long Q = (Pp * e[1] + 31) & ~31LL;
-            if (Q * e[2] * words <= t.cap) {
-                P = Pp;
-            } else {
-                Q = (P * e[1] + 3) & ~3LL;
+            long long P = 0, Q = 0;
+            box.wsc = 0;
+            if constexpr (WSCATTER) {
+                if (e[0] * e[1] * e[2] < nv_tile) {
+                    scatter_pitch<DP>(e[0], e[1], P, Q);
+                    if (Q * e[2] * words + rec_floats <= t.cap) box.wsc = 1;
+                }
+            }
+            if (!box.wsc) {
+                P = (e[0] + 3) & ~3LL;
+                long long Pp = P + (((t.pmod - (int)(P & 31)) + 32) & 31);
+                Q = (Pp * e[1] + 31) & ~31LL;
+                if (Q * e[2] * words <= t.cap) {
+                    P = Pp;
+                } else {
+                    Q = (P * e[1] + 3) & ~3LL;
+                }
             }
             long long size = Q * e[2];
             const bool fits = e[0] <= 4096 && e[1] <= 4096 && e[2] <= 4096 && size * words <= t.cap;
@@ -1093,6 +1145,81 @@ __device__ __forceinline__ void push_scatter(const WT& wx, const WT& wy, const W
     }
 }
 
+// Push ops and degrees that scatter one voxel per warp instruction: plain push
+// at DP = 3 and 4 (a degree-4 box would need pitches of 37 elements or more).
+template <int DP, int OP>
+__host__ __device__ constexpr bool warp_scatter() {
+    return OP == kPush && (DP == 3 || DP == 4);
+}
+
+// Warp-cooperative scatter of a tile's recorded voxels into the fixed-point
+// (or, when !fixed, float) accumulator: warp w takes voxels w, w + 8, ...; lane
+// l of pass p adds tap t = 32 p + l of that voxel.  With the box pitches chosen
+// by scatter_pitch the 32 reductions of a pass hit 32 distinct elements in 32
+// distinct banks.
+// Shared-memory reductions for the warp-cooperative scatter: no compiler memory
+// barrier, so the record loads of the next voxels can be issued ahead of them
+// (the records and the accumulator are disjoint; the phases are separated by
+// __syncthreads).
+__device__ __forceinline__ void red_s32_nb(unsigned a, int v) {
+    asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(a), "r"(v));
+}
+__device__ __forceinline__ void red_f32_nb(unsigned a, float v) {
+    asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(a), "f"(v));
+}
+
+template <int DP, int DPP, int NV>
+__device__ __forceinline__ void warp_scatter_tile(const float* rx, const float* ry, const float* rz, const int* rb,
+                                                  int P, int Q, unsigned acc_base, unsigned lo_off, bool fixed) {
+    constexpr int T = DP * DP * DP;
+    constexpr int PASSES = (T + 31) / 32;
+    constexpr int NW = kThreads / 32;
+    static_assert(NV % (2 * NW) == 0, "two voxels per warp iteration");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int ti[PASSES], tj[PASSES], tk[PASSES], off[PASSES];
+#pragma unroll
+    for (int p = 0; p < PASSES; ++p) {
+        const int tt = p * 32 + lane < T ? p * 32 + lane : 0;
+        ti[p] = tt % DP;
+        tj[p] = (tt / DP) % DP;
+        tk[p] = tt / (DP * DP);
+        off[p] = ti[p] + P * tj[p] + Q * tk[p];
+    }
+    // two voxels per iteration: all record loads first, then the reductions
+    for (int s0 = warp; s0 < NV; s0 += 2 * NW) {
+        int bv[2];
+        float y[2][PASSES];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int sidx = s0 + u * NW;
+            bv[u] = rb[sidx];
+            const float* X = rx + sidx * DPP;
+            const float* Y = ry + sidx * DPP;
+            const float* Z = rz + sidx * DPP;
+#pragma unroll
+            for (int p = 0; p < PASSES; ++p) y[u][p] = (X[ti[p]] * Y[tj[p]]) * Z[tk[p]];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (bv[u] < 0) continue;   // warp-uniform: every lane read the same record
+#pragma unroll
+            for (int p = 0; p < PASSES; ++p) {
+                if (p * 32 + lane >= T) continue;
+                const unsigned a = acc_base + 4u * (unsigned)(bv[u] + off[p]);
+                if (fixed) {
+                    // y in q1 units, |y| <= 2^22: hi = round(y), lo = round((y - hi) * 2^21)
+                    const float t1 = __fadd_rn(y[u][p], kMagic);
+                    const float r = __fsub_rn(y[u][p], __fsub_rn(t1, kMagic));
+                    red_s32_nb(a, __float_as_int(t1) - kMagicBits);
+                    red_s32_nb(a + lo_off, __float_as_int(__fmaf_rn(r, 2097152.0f, kMagic)) - kMagicBits);
+                } else {
+                    red_f32_nb(a, y[u][p]);
+                }
+            }
+        }
+    }
+}
+
 // Persistent push family.  The ring holds each tile's deformation and its
 // channel-0 values kStages tiles ahead; the tile scatters into the shared
 // accumulator and flushes it with global reductions.  The flush clears every
@@ -1106,6 +1233,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
     constexpr int ORD = OP == kPushGrad ? 1 : 0;
     constexpr int NCOMP = OP == kPushGrad ? 3 : 1;
     constexpr int NV = kThreads * V;
+    // push at degrees 2 and 3 scatters one voxel per warp instruction (see
+    // kScatterQMask); other ops and degrees one voxel per thread
+    constexpr bool WSC = warp_scatter<DP, OP>();
+    constexpr int DPP = 4;   // record stride per axis (DP <= 4 under WSC)
     __shared__ int red[8][7];
     __shared__ float sred[8];
     __shared__ Box box;
@@ -1125,6 +1256,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
     ring.slot_floats = (3 + NCOMP) * NV;
     float* accf = sm + kStages * (3 + NCOMP) * NV;
     ring.bars = smem_addr(accf + t.cap);
+    // voxel records of the warp-cooperative scatter (contracted tiles only), at
+    // the top of the accumulator budget: x weights, y weights times the scaled
+    // value, z weights, and the box-relative first tap (-1: skip)
+    constexpr int kRec = (3 * DPP + 1) * NV;
+    float* rx = accf + (WSC ? t.cap - kRec : 0);
+    float* ry = rx + DPP * NV;
+    float* rz = ry + DPP * NV;
+    int* rb = reinterpret_cast<int*>(rz + DPP * NV);
     for (int i = threadIdx.x; i < (t.cap >> 2); i += kThreads)
         reinterpret_cast<float4*>(accf)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (threadIdx.x == 0) {
@@ -1165,7 +1304,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
             }
             if (fin) bound0 += OP == kPushGrad ? 2.f * s1 : s1;
         }
-        reduce_box<DP>(mn, mx, t, g, 2, box, red, bound0);
+        reduce_box<DP, WSC>(mn, mx, t, g, 2, box, red, bound0, NV, WSC ? kRec : 0);
         if (s_abort) break;
         if (box.mode == 2) {
 #pragma unroll
@@ -1218,6 +1357,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
                 const bool fixed = E != INT_MIN;
                 FixedScale fs;
                 fs.set(fixed ? E : 0);
+                auto thread_scatter = [&]() {
 #pragma unroll
                 for (int q = 0; q < V; ++q) {
                     const IT v = tv.template index<IT>(o, q);
@@ -1245,6 +1385,45 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
                     if (fixed) push_scatter<DP, OP, true>(wx, wy, wz, w0, w1, w2, base, P4, Q4, lo_off);
                     else push_scatter<DP, OP, false>(wx, wy, wz, w0, w1, w2, base, P4, Q4, lo_off);
                 }
+                };
+                if constexpr (WSC) {
+                if (box.wsc) {
+                    const float sc = fixed ? fs.inv_q1 : 1.f;
+                    // each thread records its own voxels ...
+#pragma unroll
+                    for (int q = 0; q < V; ++q) {
+                        const IT v = tv.template index<IT>(o, q);
+                        const int lin = threadIdx.x + q * kThreads;
+                        int base = -1;
+                        float x0, x1, x2;
+                        if (v >= 0 && load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2)) {
+                            const float val = c == 0 ? slot[3 * NV + lin] : __ldg(inb + (long long)c * n1 + v);
+                            if (finitef(val)) {
+                                W3<DP, 0> wx, wy, wz;
+                                const int ox = spline_taps32<DP, 0>(x0, wx.w, wx.dw, wx.hw) - box.xo;
+                                const int oy = spline_taps32<DP, 0>(x1, wy.w, wy.dw, wy.hw) - box.lo[1];
+                                const int oz = spline_taps32<DP, 0>(x2, wz.w, wz.dw, wz.hw) - box.lo[2];
+                                base = oz * box.Q + oy * box.P + ox;
+                                const float sv = val * sc;
+#pragma unroll
+                                for (int i = 0; i < DP; ++i) {
+                                    rx[lin * DPP + i] = wx.w[i];
+                                    ry[lin * DPP + i] = wy.w[i] * sv;
+                                    rz[lin * DPP + i] = wz.w[i];
+                                }
+                            }
+                        }
+                        rb[lin] = base;
+                    }
+                    __syncthreads();   // records complete
+                    // ... then every warp scatters whole voxels, one tap per lane
+                    warp_scatter_tile<DP, DPP, NV>(rx, ry, rz, rb, box.P, box.Q, acc_base, lo_off, fixed);
+                } else {
+                    thread_scatter();
+                }
+                } else {
+                    thread_scatter();
+                }
                 __syncthreads();   // the scatter is complete
                 float* f0 = a.out + ((long long)o.b * g.nc + c) * g.n0;
                 if (fixed)
@@ -1260,6 +1439,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
                         accf[si] = 0.f;
                         return v;
                     });
+            }
+        }
+        if constexpr (WSC) {
+            if (box.mode == 1 && box.wsc) {   // the records sat in the accumulator budget: clear them
+                __syncthreads();
+                for (int i = threadIdx.x; i < kRec; i += kThreads) rx[i] = 0.f;
             }
         }
         __syncthreads();   // ring slot j is free and the accumulator is clear

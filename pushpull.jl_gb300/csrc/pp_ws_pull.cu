@@ -20,8 +20,9 @@ bool ws_supported(const LaunchArgs& a) {
     const Geometry& g = a.g;
     if (!(g.dp[0] == g.dp[1] && g.dp[1] == g.dp[2])) return false;
     // most of a tile inside the sample grid (degenerate grids go per voxel)
-    if (2 * g.d1[0] < 8 || 2 * g.d1[1] < 8 || 2 * g.d1[2] < 16) return false;
-    const long long ntx = (g.d1[0] + 7) >> 3, nty = (g.d1[1] + 7) >> 3, ntz = (g.d1[2] + 15) >> 4;
+    if (2 * g.d1[0] < 8 || 2 * g.d1[1] < 8 || 2 * g.d1[2] < kWsTz) return false;
+    if (g.d1[0] > 0x7fffffffLL || g.d1[1] > 0x7fffffffLL || g.d1[2] > 0x7fffffffLL) return false;
+    const long long ntx = (g.d1[0] + 7) >> 3, nty = (g.d1[1] + 7) >> 3, ntz = (g.d1[2] + kWsTz - 1) / kWsTz;
     return ntx * nty * ntz * g.nb < 0x7fffffffLL;
 }
 
@@ -29,10 +30,10 @@ bool ws_supported(const LaunchArgs& a) {
 // cannot be streamed by TMA (unaligned base or x extent), so the caller can
 // fall back to the other kernels.
 cudaError_t launch_ws_pull(int op, const LaunchArgs& a, cudaStream_t s) {
-    const TileGrid t = make_grid(a, TileCfg{kWsLx, kWsLy, kWsLz, kWsCap});
+    const TileGrid t = ws_make_grid(a);
     CUtensorMap phimap;
     std::memset(&phimap, 0, sizeof phimap);
-    if (!encode_tile_map(&phimap, a.phi, a.g.d1, 3LL * a.g.nb, t, 3)) return cudaErrorNotSupported;
+    if (!encode_ws_phi_map(&phimap, a.phi, a.g.d1, 3LL * a.g.nb)) return cudaErrorNotSupported;
     const bool small = a.g.n0 < (1LL << 31) - 1 && a.g.n1 < (1LL << 31) - 1;
     if (op == kPull) return small ? ws_dispatch<kPull, int>(a, t, phimap, s) : ws_dispatch<kPull, long long>(a, t, phimap, s);
     if (op == kPullGrad)
