@@ -472,6 +472,52 @@ __device__ __forceinline__ void flush_box(const Box& box, const Geometry& g, int
     });
 }
 
+// Flush (and clear) a two-word fixed-point accumulator box into the image.
+// Rows of an x-interior box of an aligned image go as 16-byte groups: both
+// words of 4 elements in two 16-byte loads, cleared by two 16-byte stores, one
+// 4-wide global reduction (all-zero groups skipped).  Other boxes: the
+// element-wise walk.
+template <typename IT>
+__device__ __forceinline__ void flush_fixed(const Box& box, const Geometry& g, int b0, int b1, int b2, float* f0,
+                                            int* acc_hi, int* acc_lo, const FixedScale& fs) {
+    const bool vec = (box.interior & 1) && (g.d0[0] & 3) == 0 && (reinterpret_cast<uintptr_t>(f0) & 15) == 0 &&
+                     ((box.P | box.Q | box.size) & 3) == 0;
+    if (!vec) {
+        flush_box<IT>(box, g, b0, b1, b2, f0, [&](int si) {
+            const float v = fixed_value(acc_hi[si], acc_lo[si], fs);
+            acc_hi[si] = 0;
+            acc_lo[si] = 0;
+            return v;
+        });
+        return;
+    }
+    const int ey = box.ext[1], ez = box.ext[2];
+    const int n4 = (box.ext[0] + 3) >> 2;
+    RowWalk rw(n4, ey);
+    if (rw.e0 >= n4) return;   // lanes per row >= n4: at most one group of each row per thread
+    const IT sy = (IT)g.d0[0];
+    const IT sz = (IT)(g.d0[0] * g.d0[1]);
+    const int e = 4 * rw.e0;
+    for (; rw.rz < ez; rw.next()) {
+        const int rz = rw.rz, ry = rw.ry;
+        const int si = rz * box.Q + ry * box.P + e;
+        const int4 h = *reinterpret_cast<const int4*>(acc_hi + si);
+        const int4 l = *reinterpret_cast<const int4*>(acc_lo + si);
+        *reinterpret_cast<int4*>(acc_hi + si) = make_int4(0, 0, 0, 0);
+        *reinterpret_cast<int4*>(acc_lo + si) = make_int4(0, 0, 0, 0);
+        if ((h.x | h.y | h.z | h.w | l.x | l.y | l.z | l.w) == 0) continue;
+        float sgy = 1.f, sgz = 1.f;
+        const IT gy = (box.interior & 2) ? (IT)(box.lo[1] + ry)
+                                         : (IT)fold_tap(b1, (long long)box.lo[1] + ry, g.d0[1], sgy);
+        const IT gz = (box.interior & 4) ? (IT)(box.lo[2] + rz)
+                                         : (IT)fold_tap(b2, (long long)box.lo[2] + rz, g.d0[2], sgz);
+        const float sg = sgy * sgz;
+        const float4 v = make_float4(sg * fixed_value(h.x, l.x, fs), sg * fixed_value(h.y, l.y, fs),
+                                     sg * fixed_value(h.z, l.z, fs), sg * fixed_value(h.w, l.w, fs));
+        atomicAdd(reinterpret_cast<float4*>(f0 + (gz * sz + gy * sy + (IT)box.xo) + e), v);
+    }
+}
+
 // ---- tiles -----------------------------------------------------------------
 struct TileOrigin {
     int b;            // batch
@@ -1427,12 +1473,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
                 __syncthreads();   // the scatter is complete
                 float* f0 = a.out + ((long long)o.b * g.nc + c) * g.n0;
                 if (fixed)
-                    flush_box<IT>(box, g, b0, b1, b2, f0, [&](int si) {
-                        const float v = fixed_value(acc_hi[si], acc_lo[si], fs);
-                        acc_hi[si] = 0;
-                        acc_lo[si] = 0;
-                        return v;
-                    });
+                    flush_fixed<IT>(box, g, b0, b1, b2, f0, acc_hi, acc_lo, fs);
                 else
                     flush_box<IT>(box, g, b0, b1, b2, f0, [&](int si) {
                         const float v = accf[si];
@@ -1689,12 +1730,7 @@ __global__ void __launch_bounds__(kThreads, DP <= 3 ? 3 : 2) k_fused_tiled(const
             if (box.mode == 1 && E != INT_MAX) {
                 float* df = a.out + ((long long)o.b * g.nc + c) * g.n0;
                 if (fixed)
-                    flush_box<IT>(box, g, b0, b1, b2, df, [&](int si) {
-                        const float v = fixed_value(acc_hi[si], acc_lo[si], fs);
-                        acc_hi[si] = 0;
-                        acc_lo[si] = 0;
-                        return v;
-                    });
+                    flush_fixed<IT>(box, g, b0, b1, b2, df, acc_hi, acc_lo, fs);
                 else
                     flush_box<IT>(box, g, b0, b1, b2, df, [&](int si) {
                         const float v = accf[si];
