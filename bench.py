@@ -32,6 +32,16 @@ sys.path.insert(0, ROOT)
 
 METRIC = "pull+push Gvox/s & HBM GB/s @192³ cubic; fused fwd+adjoint vs plain GPU"
 L2_FLUSH_BYTES = 256 << 20
+# GPU cycles of a spin kernel queued after each L2 flush and before the start
+# event: the host enqueues the timed calls meanwhile, so the events bracket
+# device work only (host-side argument handling is timed by the e2e leg)
+HOST_AHEAD_CYCLES = 400_000
+
+
+def _flush(buf):
+    import torch
+    buf.fill_(1.0)
+    torch.cuda._sleep(HOST_AHEAD_CYCLES)
 
 
 def _peaks():
@@ -65,9 +75,10 @@ def _oracle_threads():
     return max(1, min(32, os.cpu_count() or 1))
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each kernel
-# on this workload, from one ncu capture (profiles/k_pull_tiled_192cubic.md, profiles/k_push_tiled_192cubic.md).
-TRAFFIC = {"pull": 126_790_144, "push": 152_880_128}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each kernel on this
+# workload, from one ncu capture each (profiles/k_pull_ws_192cubic.md, k_push_tiled_192cubic.md,
+# k_pull_ws_affine_192cubic.md, k_push_tiled_affine_192cubic.md)
+TRAFFIC = {"pull": 126_495_488, "push": 152_941_824, "affine_pull": 28_766_464, "affine_push": 56_648_448}
 
 
 class Clocks:
@@ -188,7 +199,9 @@ def _config(w, args):
                         "scaled to +-5 vox",
             "d": list(w.f0.shape[:3]), "deg": list(w.deg), "bnd": w.bnd, "ext": w.ext, "channels": 1,
             "seed": args.seed,
-            "l2": f"flushed before every step by a {L2_FLUSH_BYTES >> 20} MiB write outside the step's events"}
+            "l2": f"flushed before every step by a {L2_FLUSH_BYTES >> 20} MiB write outside the step's events",
+            "timing": f"CUDA events on the launch stream; a {HOST_AHEAD_CYCLES}-cycle GPU spin before each start "
+                      "event lets the host enqueue the step first, so the events bracket device work"}
 
 
 def run_gpu(args):
@@ -217,7 +230,7 @@ def run_gpu(args):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
     def step(evs=None):
-        flush.fill_(1.0)
+        _flush(flush)
         if evs:
             evs[0].record()
         pkg.pull(f0, phi, s, out=f1)
@@ -251,7 +264,7 @@ def run_gpu(args):
     g1 = L.empty(d1 + (3,), device=dev)
     pg_ms = []
     for i in range(max(args.steps, 5) + 3):
-        flush.fill_(1.0)
+        _flush(flush)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         pkg.pull_grad(f0, phi, s, out=g1)
@@ -260,6 +273,15 @@ def run_gpu(args):
         if i >= 3:
             pg_ms.append(e0.elapsed_time(e1))
     del g1
+    # affine pull and push of the same image (positions A (i, j, k, 1) computed
+    # in the kernels in place of a deformation), outside the timed step
+    from pushpull_gb300 import workloads as W
+    Aff = W.affine_map(d0, seed=args.seed + 4)
+    fa = L.empty(d1, device=dev)
+    aa = L.empty(d0, device=dev)
+    reps = max(args.steps, 5)
+    aff_pull_ms = _timeit(lambda: pkg.affine_pull(f0, Aff, d1, s, out=fa), reps, flush)
+    aff_push_ms = _timeit(lambda: pkg.affine_push(fa, Aff, d0, s, out=aa), reps, flush)
     # FP64 error of the benchmarked pull and push (outside every timed region):
     # f1 and acc hold the last timed step's outputs
     accuracy = None
@@ -268,8 +290,11 @@ def run_gpu(args):
         so = O.Sett.make(w.deg, w.bnd, w.ext)
         th = _oracle_threads()
         f1n = L.to_numpy(f1)
+        fan = L.to_numpy(fa)
         accuracy = {"pull": _errors(f1n, O.pull(w.f0, w.phi, so, threads=th)),
                     "push": _errors(L.to_numpy(acc), O.push(f1n, w.phi, d0, so, threads=th)),
+                    "affine_pull": _errors(fan, O.pull_affine(w.f0, Aff, d1, so)),
+                    "affine_push": _errors(L.to_numpy(aa), O.push_affine(fan, Aff, d0, so)),
                     "reference": "FP64 oracle (oracle/pp_oracle.c) on the same inputs, whole volume"}
     pull_ms = [e[0].elapsed_time(e[1]) for e in evs]
     push_ms = [e[1].elapsed_time(e[2]) for e in evs]
@@ -347,10 +372,16 @@ def run_gpu(args):
     bytes_pg = 12 * n1 + 4 * nc * n0 + 12 * nc * n1
     kernels["pull_grad"] = {"ms": mg, "GB_s": bytes_pg / (mg * 1e-3) / 1e9,
                             "frac_of_peak": bytes_pg / (mg * 1e-3) / 1e9 / peak, "Gvox_s": n1 / (mg * 1e-3) / 1e9}
-    for k in ("pull", "push", "pull_grad"):
+    bytes_aff = 4 * nc * n0 + 4 * nc * n1
+    for k, ms in (("affine_pull", aff_pull_ms), ("affine_push", aff_push_ms)):
+        kernels[k] = {"ms": ms, "GB_s": bytes_aff / (ms * 1e-3) / 1e9,
+                      "frac_of_peak": bytes_aff / (ms * 1e-3) / 1e9 / peak, "Gvox_s": n1 / (ms * 1e-3) / 1e9}
+    kernels["affine_map"] = [[float(v) for v in row] for row in Aff]
+    for k in ("pull", "push", "pull_grad", "affine_pull", "affine_push"):
         kernels[k]["traffic_bytes_ncu"] = TRAFFIC.get(k)
     kernels["bytes_model"] = ("algorithmic bytes per launch: pull 12 n1 (phi) + 4 n0 (image, once) + 4 n1 (out); "
-                              "push 12 n1 + 4 n1 (values) + 4 n0 (image written once); pull_grad 12 n1 + 4 n0 + 12 n1")
+                              "push 12 n1 + 4 n1 (values) + 4 n0 (image written once); pull_grad 12 n1 + 4 n0 + 12 n1; "
+                              "affine pull 4 n0 + 4 n1, affine push 4 n1 + 4 n0 (no deformation)")
     cpu = None
     if not args.no_cpu and ws == 1 or (not args.no_cpu and rank == 0):
         cpu, _ = cpu_baseline(w, seconds=args.cpu_seconds)
@@ -402,7 +433,7 @@ def fused_vs_plain(pkg, dev, args):
             fn()
         ms = []
         for _ in range(reps):
-            flush.fill_(1.0)
+            _flush(flush)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             fn()
@@ -454,7 +485,7 @@ def _timeit(fn, reps, flush):
         fn()
     ms = []
     for _ in range(reps):
-        flush.fill_(1.0)
+        _flush(flush)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         fn()
@@ -554,6 +585,61 @@ def contention_leg(pkg, dev, args):
             "accuracy_vs_fp64": accuracy}
 
 
+PROFILE_CASES = ("pull", "pull_grad", "push", "affine_pull", "affine_push", "contention_push",
+                 "contention_push_grad", "fused")
+
+
+def run_profile(args):
+    """Launch one op on its benchmark workload --warmup + --steps times, untimed:
+    the program the ncu captures run (192^3 cubic for pull, pull_grad, push and the
+    affine ops; the 256^3 x 3 contraction for contention_*; the 160x192x160
+    quadratic step for fused)."""
+    import torch
+    import __graft_entry__ as entry
+    from pushpull_gb300 import workloads as W
+    pkg = entry.package()
+    L = pkg.layout
+    dev = torch.device("cuda", 0)
+    case = args.profile
+    if case.startswith("contention"):
+        d = (256, 256, 256)
+        s = pkg.Settings(3, 1, 1)
+        phi = W.deformation_gpu(d, 53, fwhm=12.0, amplitude=3.0, contraction=0.25, device=dev)
+        out = L.empty(d + (3,), device=dev)
+        if case == "contention_push":
+            f1 = W.image_gpu(d, 51, fwhm=3.0, channels=3, device=dev)
+            fn = lambda: pkg.push(f1, phi, d, s, out=out, accumulate=False)   # noqa: E731
+        else:
+            g1 = L.empty(d + (3, 3), device=dev)
+            g1.copy_(torch.randn(g1.shape, generator=torch.Generator(device=dev).manual_seed(52), device=dev))
+            fn = lambda: pkg.push_grad(g1, phi, d, s, out=out, accumulate=False)   # noqa: E731
+    elif case == "fused":
+        w = W.config3(seed=args.seed + 1)
+        s = pkg.Settings(w.deg, w.bnd, w.ext)
+        f0, phi = L.from_numpy(w.f0, dev), L.from_numpy(w.phi, dev)
+        g = pkg.pull(f0, L.from_numpy(w.extra["phi2"], dev), s)
+        fn = lambda: pkg.fused_step(f0, phi, g, s)   # noqa: E731
+    else:
+        w = _workload(args)
+        s = pkg.Settings(w.deg, w.bnd, w.ext)
+        d0, d1 = tuple(w.f0.shape[:3]), tuple(w.phi.shape[:3])
+        f0, phi = L.from_numpy(w.f0, dev), L.from_numpy(w.phi, dev)
+        f1 = pkg.pull(f0, phi, s)
+        Aff = W.affine_map(d0, seed=args.seed + 4)
+        out0, out1, outg = L.empty(d0, device=dev), L.empty(d1, device=dev), L.empty(d1 + (3,), device=dev)
+        fn = {"pull": lambda: pkg.pull(f0, phi, s, out=out1),
+              "pull_grad": lambda: pkg.pull_grad(f0, phi, s, out=outg),
+              "push": lambda: pkg.push(f1, phi, d0, s, out=out0, accumulate=False),
+              "affine_pull": lambda: pkg.affine_pull(f0, Aff, d1, s, out=out1),
+              "affine_push": lambda: pkg.affine_push(f1, Aff, d0, s, out=out0)}[case]
+    for _ in range(args.warmup + args.steps):
+        fn()
+    torch.cuda.synchronize()
+    status = int(pkg.native_library().pp_device_status(1))
+    print(json.dumps({"profile": case, "launches": args.warmup + args.steps, "device_status": status}))
+    return 0 if status == 0 else 1
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -568,9 +654,13 @@ def main(argv=None):
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-contention", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 error fields")
+    ap.add_argument("--profile", choices=PROFILE_CASES, default=None,
+                    help="launch one op warmup + steps times without timing (for ncu captures)")
     args = ap.parse_args(argv)
     import __graft_entry__ as entry
     entry.package()
+    if args.profile:
+        return run_profile(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

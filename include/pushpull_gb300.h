@@ -169,7 +169,10 @@ int pp_fused_step_noalloc(double *loss, float *df, float *dphi, const float *f0,
  * reference's adjust_affine, src/pushpull_cpu.jl:357-362); it is passed to the
  * kernel by value.  Positions are rounded exactly as the reference CPU code
  * (xj = Aff[3]*j + Aff[6]*k + Aff[9], then x = xj + Aff[0]*i).  Validity, NaN
- * and skipping rules as pp_pull / pp_push.  Replaces affine_pull_element /
+ * and skipping rules as pp_pull / pp_push.  Isotropic degrees run on the tiled
+ * kernels of pp_pull / pp_push with the positions computed in place (the tile
+ * registry's pull and push entries decide, as for the deformation ops); other
+ * settings on per-voxel kernels.  Replaces affine_pull_element /
  * affine_push_element (artifacts/C/pushpull.cu:187-231) and the per-slice
  * ccall loops of src/pushpull_cpu.jl:268-349. */
 int pp_pull_affine(float *f1, const float *f0, const float *Aff, const pp_usize d0[3], const pp_usize d1[3],
@@ -180,17 +183,22 @@ int pp_push_affine(float *f0, const float *f1, const float *Aff, const pp_usize 
 
 /* ---- batched uneven workload ------------------------------------------- */
 /* One (image, deformation) pair of a batch: f1 = pull(f0, phi) is written and
- * out (+)= push(f1, phi) is accumulated, all device pointers, single batch,
- * isotropic degree.  Items may differ in size, channels, degree and bounds
- * (e.g. registration pairs and their multigrid pyramid levels). */
+ * out (+)= push(f1, phi) is accumulated, all device pointers, single batch.
+ * Items may differ in size, channels, degrees and bounds (e.g. registration
+ * pairs and their multigrid pyramid levels), as the reference's per-array
+ * calls allow (src/pushpull_general.jl:33-54, ext/pushpull_gpu.jl:37-49).
+ * Zero-initialised trailing fields keep the isotropic, one-triple form. */
 typedef struct {
     const float *f0;      /* (d0, nc)     */
     const float *phi;     /* (d1, 3)      */
     float *f1;            /* (d1, nc)     */
     float *out;           /* (d0, nc)     */
     pp_usize d0[3], d1[3];
-    int nc, deg;          /* channels, isotropic degree 0..4 */
-    int bnd[3], ext;      /* boundary codes (all channels), extrapolate */
+    int nc, deg;          /* channels; degree 0..4 in every dimension, or -1: per dimension in deg3 */
+    int bnd[3], ext;      /* boundary codes (every channel unless nbnd > 1), extrapolate */
+    int deg3[3];          /* per-dimension degrees when deg == -1 */
+    int nbnd;             /* 0 or 1: bnd for every channel; nc: per-channel triples in bnds */
+    const int *bnds;      /* host, 3 * nbnd codes (channel-major) when nbnd > 1 */
 } pp_batch_item;
 
 typedef struct pp_batch pp_batch;

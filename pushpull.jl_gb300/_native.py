@@ -28,7 +28,7 @@ class BatchItem(C.Structure):
     """pp_batch_item of include/pushpull_gb300.h."""
     _fields_ = [("f0", _vp), ("phi", _vp), ("f1", _vp), ("out", _vp), ("d0", C.c_ulonglong * 3),
                 ("d1", C.c_ulonglong * 3), ("nc", C.c_int), ("deg", C.c_int), ("bnd", C.c_int * 3),
-                ("ext", C.c_int)]
+                ("ext", C.c_int), ("deg3", C.c_int * 3), ("nbnd", C.c_int), ("bnds", _vp)]
 
 
 # name -> (restype, argtypes)

@@ -15,8 +15,8 @@ from .settings import Settings
 
 class BatchPlan:
     """``items``: dicts with ``f0 (d0[, C])``, ``phi (d1, 3)``, ``f1 (d1[, C])``,
-    ``out (d0[, C])`` (column-major CUDA float32 tensors) and ``sett`` (isotropic
-    degree; one boundary triple for all channels)."""
+    ``out (d0[, C])`` (column-major CUDA float32 tensors) and ``sett`` (any
+    per-dimension degrees; one boundary triple, or one per channel)."""
 
     def __init__(self, items, zero_outputs: bool = True):
         self._lib = _native.lib()
@@ -28,16 +28,21 @@ class BatchPlan:
                 if t.device.type != "cuda" or t.dtype != torch.float32:
                     raise TypeError("batch arrays must be CUDA float32 tensors")
             s: Settings = it["sett"]
-            assert s.deg[0] == s.deg[1] == s.deg[2], "batch items need an isotropic degree"
-            assert len(s.bnd) == 1, "batch items take one boundary triple"
-            self._keep += [f0, phi, f1, out]
             nc = L.jsize(f0, 4)
+            assert len(s.bnd) in (1, nc), "one boundary triple, or one per channel"
+            self._keep += [f0, phi, f1, out]
             e = arr[i]
             e.f0, e.phi, e.f1, e.out = f0.data_ptr(), phi.data_ptr(), f1.data_ptr(), out.data_ptr()
             e.d0 = (C.c_ulonglong * 3)(*f0.shape[:3])
             e.d1 = (C.c_ulonglong * 3)(*phi.shape[:3])
-            e.nc, e.deg, e.ext = nc, s.deg[0], s.ext
+            iso = s.deg[0] == s.deg[1] == s.deg[2]
+            e.nc, e.deg, e.ext = nc, s.deg[0] if iso else -1, s.ext
+            e.deg3 = (C.c_int * 3)(*s.deg)
             e.bnd = (C.c_int * 3)(*s.bnd[0])
+            if len(s.bnd) > 1:
+                codes = (C.c_int * (3 * nc))(*[v for b in s.bnd for v in b])   # read by pp_batch_create
+                self._keep.append(codes)
+                e.nbnd, e.bnds = nc, C.cast(codes, C.c_void_p)
         self._h = C.c_void_p()
         _native.check("pp_batch_create", self._lib.pp_batch_create(C.byref(self._h), arr, len(items),
                                                                     int(bool(zero_outputs))))

@@ -3,74 +3,61 @@
 // (0-based, the matrix already adjusted from the 1-based convention), so the
 // kernels read only the image (pull) or the values (push): 8 bytes per voxel.
 //
+// Isotropic degrees 1..4 run on the tiled kernels with the positions computed
+// in place: the warp-specialised pull (pp_ws.cuh) and the tiled push
+// (pp_tiled_impl.cuh, pp_tiled_affine.cu), whose footprint boxes an affine map
+// keeps regular.  The per-voxel kernels below take everything else
+// (anisotropic degrees, degenerate grids, or the direct path).
+//
 // Reference: affine_pull_element / affine_push_element (artifacts/C/pushpull.cu:
 // 187-231) and the CPU pull_affine / push_affine (artifacts/C/pushpull.c:176-243),
 // whose rounding of the position this follows: xj = A[3]*j + A[6]*k + A[9],
 // then x = xj + A[0]*i, every operation rounded separately.
+#include "pp_tiled.cuh"
 #include "pp_voxel.cuh"
 #include "pushpull_gb300.h"
 
 namespace pp {
 namespace {
 
-struct Affine {
-    float m[12];   // column-major 3x4, 0-based
-};
-
-// 0-based position of voxel v of the d1 grid, rounded as the reference CPU code
+// 0-based position of voxel v of the d1 grid
 template <typename IT>
-__device__ __forceinline__ void affine_position(const Affine& A, IT v, IT d1x, IT d1y, float& x0, float& x1,
-                                                float& x2) {
+__device__ __forceinline__ void voxel_position(const AffineMap& A, IT v, IT d1x, IT d1y, float& x0, float& x1,
+                                               float& x2) {
     const IT jk = v / d1x;
     const IT i = v - jk * d1x;
     const IT k = jk / d1y;
     const IT j = jk - k * d1y;
-    const float fi = (float)i, fj = (float)j, fk = (float)k;
-    float x[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const float xj = __fadd_rn(__fadd_rn(__fmul_rn(A.m[3 + c], fj), __fmul_rn(A.m[6 + c], fk)), A.m[9 + c]);
-        x[c] = __fadd_rn(xj, __fmul_rn(A.m[c], fi));
-    }
-    x0 = x[0];
-    x1 = x[1];
-    x2 = x[2];
-}
-
-// the reference's VOXOK on a 0-based position (artifacts/C/pushpull.c:6-9)
-__device__ __forceinline__ bool position_valid(float x0, float x1, float x2, const Geometry& g) {
-    if (!(finitef(x0) && finitef(x1) && finitef(x2))) return false;
-    if (g.ext) return true;
-    return x0 >= -0.01f && x0 <= g.hi[0] && x1 >= -0.01f && x1 <= g.hi[1] && x2 >= -0.01f && x2 <= g.hi[2];
+    affine_position(A, (float)i, (float)j, (float)k, x0, x1, x2);
 }
 
 template <int DP, typename IT>
-__global__ void __launch_bounds__(256) k_affine_pull(LaunchArgs a, Affine A) {
+__global__ void __launch_bounds__(256) k_affine_pull(LaunchArgs a, AffineMap A) {
     const Geometry& g = a.g;
     const IT n1 = (IT)g.n1, d1x = (IT)g.d1[0], d1y = (IT)g.d1[1];
     const int b = blockIdx.y;
     for (IT v = (IT)blockIdx.x * blockDim.x + threadIdx.x; v < n1; v += (IT)gridDim.x * blockDim.x) {
         float x0, x1, x2;
-        affine_position<IT>(A, v, d1x, d1y, x0, x1, x2);
+        voxel_position<IT>(A, v, d1x, d1y, x0, x1, x2);
         if (!position_valid(x0, x1, x2, g)) pull_voxel_nan<kPull>(a, b, (long long)v);
         else pull_voxel_global<DP, kPull, IT>(a, b, (long long)v, x0, x1, x2);
     }
 }
 
 template <int DP, typename IT>
-__global__ void __launch_bounds__(256) k_affine_push(LaunchArgs a, Affine A) {
+__global__ void __launch_bounds__(256) k_affine_push(LaunchArgs a, AffineMap A) {
     const Geometry& g = a.g;
     const IT n1 = (IT)g.n1, d1x = (IT)g.d1[0], d1y = (IT)g.d1[1];
     const int b = blockIdx.y;
     for (IT v = (IT)blockIdx.x * blockDim.x + threadIdx.x; v < n1; v += (IT)gridDim.x * blockDim.x) {
         float x0, x1, x2;
-        affine_position<IT>(A, v, d1x, d1y, x0, x1, x2);
+        voxel_position<IT>(A, v, d1x, d1y, x0, x1, x2);
         if (position_valid(x0, x1, x2, g)) push_voxel_global<DP, kPush, IT>(a, b, (long long)v, x0, x1, x2);
     }
 }
 
 template <typename IT>
-cudaError_t launch_affine_it(bool push, const LaunchArgs& a, const Affine& A, dim3 grid, cudaStream_t s) {
+cudaError_t launch_affine_it(bool push, const LaunchArgs& a, const AffineMap& A, dim3 grid, cudaStream_t s) {
     const int d = a.g.dp[0];
     const bool iso = a.g.dp[1] == d && a.g.dp[2] == d;
 #define PP_AFF_CASE(DPV)                                                           \
@@ -94,6 +81,8 @@ cudaError_t launch_affine_it(bool push, const LaunchArgs& a, const Affine& A, di
 }  // namespace
 
 int fail_status(int code, const char* fmt, ...);
+TileCfg tile_for(int op_index, int deg);
+int current_path();
 int prepare_args(LaunchArgs& a, float* out, const float* phi, const float* in, const pp_usize d0[3],
                  const pp_usize d1[3], int nc, int nb, const int* bnd, int nbnd, const int deg[3], int ext);
 
@@ -112,8 +101,22 @@ int run_affine(bool push, float* out, const float* in, const float* Aff, const p
         if (e != cudaSuccess) return fail_status(PP_ERR_CUDA, "zero output: %s", cudaGetErrorString(e));
     }
     if (a.g.n1 == 0) return PP_OK;
-    Affine A;
+    AffineMap A;
     for (int q = 0; q < 12; ++q) A.m[q] = Aff[q];
+    e = cudaErrorNotSupported;
+    if (current_path() != PP_PATH_DIRECT) {
+        // the registry's pull (op 0) and push (op 3) entries decide, as for the
+        // deformation ops: a zero budget means the per-voxel kernels
+        if (!push) {
+            if (tile_for(0, deg[0]).cap > 0 && ws_supported(a)) e = launch_ws_pull_affine(a, A, s);
+        } else {
+            const TileCfg t = tile_for(3, deg[0]);
+            if (t.cap > 0 && tiled_supported(a, t)) e = launch_push_tiled_affine(a, t, A, s);
+        }
+        if (e == cudaErrorNotSupported) (void)cudaGetLastError();
+        else if (e != cudaSuccess) return fail_status(PP_ERR_CUDA, "affine launch: %s", cudaGetErrorString(e));
+        else return PP_OK;
+    }
     const long long blocks_needed = (a.g.n1 + 255) / 256;
     const long long cap = (long long)sm_count() * 8;
     const dim3 grid((unsigned)(blocks_needed < cap ? blocks_needed : cap), (unsigned)a.g.nb);

@@ -20,13 +20,17 @@ int prepare_args(LaunchArgs& a, float* out, const float* phi, const float* in, c
 TileCfg tile_for(int op_index, int deg);
 }  // namespace pp
 
+// Shared-memory budget of the batched kernel, in floats: three words per box
+// element (two accumulator words, one image word).
+constexpr int kBatchCap = 24576;
+
 struct pp_batch {
     int device = -1;
     std::vector<pp::BatchItem> items;
     pp::BatchItem* dev_items = nullptr;
     unsigned* counter = nullptr;
     int total = 0;
-    int cap = 24576;
+    int cap = kBatchCap;
     bool zero_outputs = false;
     std::vector<std::pair<float*, size_t>> outputs;   // (pointer, bytes) zeroed before each run
     cudaGraph_t graph = nullptr;
@@ -76,12 +80,21 @@ int pp_batch_create(pp_batch** plan, const pp_batch_item* items, int n, int zero
     long long total = 0;
     for (int i = 0; i < n; ++i) {
         const pp_batch_item& it = items[i];
-        const int deg[3] = {it.deg, it.deg, it.deg};
+        const bool per_dim = it.deg == -1;
+        const int deg[3] = {per_dim ? it.deg3[0] : it.deg, per_dim ? it.deg3[1] : it.deg,
+                            per_dim ? it.deg3[2] : it.deg};
+        const bool per_chan = it.nbnd > 1;
+        if (per_chan && !it.bnds) {
+            delete p;
+            return pp::fail_status(PP_ERR_NULL, "batch item %d: nbnd > 1 needs bnds", i);
+        }
+        const int* bnd = per_chan ? it.bnds : it.bnd;
+        const int nbnd = per_chan ? it.nbnd : 1;
         pp::BatchItem bi;
         std::memset(&bi, 0, sizeof bi);
-        int rc = pp::prepare_args(bi.pull, it.f1, it.phi, it.f0, it.d0, it.d1, it.nc, 1, it.bnd, 1, deg, it.ext);
+        int rc = pp::prepare_args(bi.pull, it.f1, it.phi, it.f0, it.d0, it.d1, it.nc, 1, bnd, nbnd, deg, it.ext);
         if (rc == PP_OK)
-            rc = pp::prepare_args(bi.push, it.out, it.phi, it.f1, it.d0, it.d1, it.nc, 1, it.bnd, 1, deg, it.ext);
+            rc = pp::prepare_args(bi.push, it.out, it.phi, it.f1, it.d0, it.d1, it.nc, 1, bnd, nbnd, deg, it.ext);
         if (rc != PP_OK) {
             delete p;
             return rc;
@@ -91,10 +104,16 @@ int pp_batch_create(pp_batch** plan, const pp_batch_item* items, int n, int zero
             delete p;
             return pp::fail_status(PP_ERR_TOO_LARGE, "batch item %d exceeds 2^31 voxels", i);
         }
-        const pp::TileCfg tc = batch_tile_for(it.d1, it.deg);
+        const bool iso = deg[0] == deg[1] && deg[1] == deg[2];
+        const pp::TileCfg tc = batch_tile_for(it.d1, deg[0]);
         bi.t = pp::tile_grid(bi.pull, tc);
-        bi.t.cap = p->cap;
-        bi.dp = it.deg + 1;
+        // the push registry entry of the degree sets the box budget (two words per
+        // element there, three here), within the kernel's fixed budget
+        const pp::TileCfg pc = pp::tile_for(PP_OP_PUSH, deg[0]);
+        const long long want = pc.cap > 0 ? (3LL * pc.cap / 2) & ~3LL : p->cap;
+        bi.t.cap = (int)(want < 64 ? 64 : (want > p->cap ? p->cap : want));
+        // anisotropic degrees: the per-voxel path of the batched kernel (dp 0)
+        bi.dp = iso ? deg[0] + 1 : 0;
         bi.tile_begin = (int)total;
         total += (long long)bi.t.ntiles;
         if (total >= (1LL << 31) - 1) {

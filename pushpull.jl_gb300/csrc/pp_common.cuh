@@ -55,15 +55,41 @@ __device__ __forceinline__ void red_shared_f32(unsigned a, float v) {
     asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
 }
 
+// The validity test (VOXOK) of a 0-based position.
+__device__ __forceinline__ bool position_valid(float x0, float x1, float x2, const Geometry& g) {
+    if (!(finitef(x0) && finitef(x1) && finitef(x2))) return false;
+    if (g.ext) return true;
+    return x0 >= -0.01f && x0 <= g.hi[0] && x1 >= -0.01f && x1 <= g.hi[1] && x2 >= -0.01f && x2 <= g.hi[2];
+}
+
 // x = phi - 1 and the validity test, exactly as the reference evaluates them.
 __device__ __forceinline__ bool load_valid(float p0, float p1, float p2, const Geometry& g,
                                            float& x0, float& x1, float& x2) {
     x0 = __fsub_rn(p0, 1.0f);
     x1 = __fsub_rn(p1, 1.0f);
     x2 = __fsub_rn(p2, 1.0f);
-    if (!(finitef(x0) && finitef(x1) && finitef(x2))) return false;
-    if (g.ext) return true;
-    return x0 >= -0.01f && x0 <= g.hi[0] && x1 >= -0.01f && x1 <= g.hi[1] && x2 >= -0.01f && x2 <= g.hi[2];
+    return position_valid(x0, x1, x2, g);
+}
+
+// A 3x4 affine map (column-major, 0-based) in place of a stored deformation.
+struct AffineMap {
+    float m[12];
+};
+
+// Position of sample voxel (i, j, k) under A, rounded as the reference CPU code
+// (artifacts/C/pushpull.c:190-200): xj = A[3+c] j + A[6+c] k + A[9+c], then
+// x = xj + A[c] i, every operation rounded separately.
+__device__ __forceinline__ void affine_position(const AffineMap& A, float fi, float fj, float fk, float& x0,
+                                                float& x1, float& x2) {
+    float x[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float xj = __fadd_rn(__fadd_rn(__fmul_rn(A.m[3 + c], fj), __fmul_rn(A.m[6 + c], fk)), A.m[9 + c]);
+        x[c] = __fadd_rn(xj, __fmul_rn(A.m[c], fi));
+    }
+    x0 = x[0];
+    x1 = x[1];
+    x2 = x[2];
 }
 
 // Map an unbounded tap index into [0, d) and return the sign the boundary rule

@@ -18,6 +18,7 @@ unsigned status_push_grad(bool reset);
 unsigned status_fused(bool reset);
 unsigned status_batch(bool reset);
 unsigned status_ws_pull(bool reset);
+unsigned status_push_affine(bool reset);
 
 bool tiled_supported(const LaunchArgs& a, const TileCfg& t) {
     const Geometry& g = a.g;
@@ -98,6 +99,7 @@ unsigned read_device_status(bool reset) {
     v |= status_fused(reset);
     v |= status_batch(reset);
     v |= status_ws_pull(reset);
+    v |= status_push_affine(reset);
     v |= unit_status(reset);   // the bounded-wait probe of this unit
     return v;
 }

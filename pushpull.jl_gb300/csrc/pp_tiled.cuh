@@ -13,12 +13,16 @@ struct TileCfg {
 };
 
 bool tiled_supported(const LaunchArgs& a, const TileCfg& t);
-// warp-specialised pull family (8 x 8 x 16 tiles, pp_ws.cuh): geometry test and
+// warp-specialised pull family (8 x 8 x 15 tiles, pp_ws.cuh): geometry test and
 // launch (cudaErrorNotSupported for ops or layouts it does not take)
 bool ws_supported(const LaunchArgs& a);
 cudaError_t launch_ws_pull(int op, const LaunchArgs& a, cudaStream_t s);
+// the affine pull on the same kernels (positions A * (i, j, k, 1) in place of a deformation)
+cudaError_t launch_ws_pull_affine(const LaunchArgs& a, const AffineMap& A, cudaStream_t s);
 cudaError_t launch_pull_tiled(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s);
 cudaError_t launch_push_tiled(int op, const LaunchArgs& a, const TileCfg& t, cudaStream_t s);
+// the affine push on the tiled push kernels (positions A * (i, j, k, 1))
+cudaError_t launch_push_tiled_affine(const LaunchArgs& a, const TileCfg& t, const AffineMap& A, cudaStream_t s);
 
 // Geometry of the tile grid, computed on the host once per launch.
 struct TileGrid {
@@ -47,7 +51,7 @@ struct BatchItem {
     LaunchArgs push;     // phi, in = f1, out = image-grid accumulator
     TileGrid t;          // 512-voxel tiles
     int tile_begin;      // first global tile index of this item
-    int dp;              // isotropic degree + 1
+    int dp;              // isotropic degree + 1; 0: per-dimension degrees (per-voxel path)
 };
 TileGrid tile_grid(const LaunchArgs& a, const TileCfg& c);
 // items in device memory; `counter` a zeroed device word for the work queue

@@ -640,8 +640,9 @@ struct Ring {
 
 // Fill ring slot (j % kStages) with tile T: deformation components 0..2 and
 // NVAL value components of channel 0 of `vals` (layout (d1, NVAL, nc, nb); the
-// push input, or the fused step's target).  Called by every thread.
-template <int V, int NVAL, bool TMA, typename IT>
+// push input, or the fused step's target).  Called by every thread.  AFF (the
+// affine ops): the values only, the deformation part of the slot stays unused.
+template <int V, int NVAL, bool TMA, typename IT, bool AFF = false>
 __device__ __forceinline__ void ring_fill(const Ring& r, int j, int T, const LaunchArgs& a, const TileGrid& t,
                                           const ThreadVox<V>& tv, const CUtensorMap& phimap,
                                           const CUtensorMap& valmap, const float* vals) {
@@ -652,21 +653,23 @@ __device__ __forceinline__ void ring_fill(const Ring& r, int j, int T, const Lau
         if (threadIdx.x == 0) {
             const unsigned bar = r.bars + 8u * (j % kStages);
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_expect_tx(bar, (unsigned)((3 + NVAL) * NV * sizeof(float)));
-            tma_load_4d(smem_addr(slot), &phimap, bar, o.x0, o.y0, o.z0, 3 * o.b);
+            mbar_expect_tx(bar, (unsigned)(((AFF ? 0 : 3) + NVAL) * NV * sizeof(float)));
+            if constexpr (!AFF) tma_load_4d(smem_addr(slot), &phimap, bar, o.x0, o.y0, o.z0, 3 * o.b);
             if constexpr (NVAL > 0)
                 tma_load_4d(smem_addr(slot + 3 * NV), &valmap, bar, o.x0, o.y0, o.z0, NVAL * a.g.nc * o.b);
         }
     } else {
         const long long n1 = a.g.n1;
-        const float* phi = a.phi + (long long)o.b * 3 * n1;
+        const float* phi = AFF ? nullptr : a.phi + (long long)o.b * 3 * n1;
         const float* val = vals + (long long)o.b * a.g.nc * NVAL * n1;
 #pragma unroll
         for (int q = 0; q < V; ++q) {
             const int lin = threadIdx.x + q * kThreads;
             const IT v = tv.template index<IT>(o, q);
+            if constexpr (!AFF) {
 #pragma unroll
-            for (int k = 0; k < 3; ++k) slot[k * NV + lin] = v < 0 ? 0.f : __ldg(phi + v + k * n1);
+                for (int k = 0; k < 3; ++k) slot[k * NV + lin] = v < 0 ? 0.f : __ldg(phi + v + k * n1);
+            }
 #pragma unroll
             for (int k = 0; k < NVAL; ++k) slot[(3 + k) * NV + lin] = v < 0 ? 0.f : __ldg(val + v + k * n1);
         }
@@ -679,11 +682,32 @@ __device__ __forceinline__ bool ring_wait(const Ring& r, int j) {
     return true;
 }
 
-// First-tap bounds of this thread's valid voxels of the tile in `slot`.
-template <int DP, int V, typename IT>
-__device__ __forceinline__ void tile_bounds(const Geometry& g, const TileOrigin& o, const ThreadVox<V>& tv,
-                                            const float* slot, int (&mn)[3], int (&mx)[3]) {
-    constexpr int NV = kThreads * V;
+// Sample positions of a tile's voxels: x = phi - 1 from the tile's ring slot,
+// or (AFF, the affine ops) A * (i, j, k, 1) from the voxel's grid coordinates;
+// either way with the validity test.
+template <int NV, bool AFF>
+struct TilePos {
+    const float* slot;
+    const AffineMap* A;
+    int lx, ly;
+    __device__ __forceinline__ bool operator()(const Geometry& g, const TileOrigin& o, int lin, float& x0, float& x1,
+                                               float& x2) const {
+        if constexpr (AFF) {
+            const int gx = o.x0 + (lin & ((1 << lx) - 1));
+            const int gy = o.y0 + ((lin >> lx) & ((1 << ly) - 1));
+            const int gz = o.z0 + (lin >> (lx + ly));
+            affine_position(*A, (float)gx, (float)gy, (float)gz, x0, x1, x2);
+            return position_valid(x0, x1, x2, g);
+        } else {
+            return load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2);
+        }
+    }
+};
+
+// First-tap bounds of this thread's valid voxels of a tile.
+template <int DP, int V, typename IT, class POS>
+__device__ __forceinline__ void tile_bounds_pos(const Geometry& g, const TileOrigin& o, const ThreadVox<V>& tv,
+                                                const POS& pos, int (&mn)[3], int (&mx)[3]) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         mn[k] = INT_MAX;
@@ -694,7 +718,7 @@ __device__ __forceinline__ void tile_bounds(const Geometry& g, const TileOrigin&
         const int lin = threadIdx.x + q * kThreads;
         if (tv.template index<IT>(o, q) < 0) continue;
         float x[3];
-        if (!load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x[0], x[1], x[2])) continue;
+        if (!pos(g, o, lin, x[0], x[1], x[2])) continue;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const int f = first_tap32(x[k], DP);
@@ -703,6 +727,13 @@ __device__ __forceinline__ void tile_bounds(const Geometry& g, const TileOrigin&
             mx[k] = max(mx[k], c);
         }
     }
+}
+
+// ... of the tile whose deformation is in `slot`.
+template <int DP, int V, typename IT>
+__device__ __forceinline__ void tile_bounds(const Geometry& g, const TileOrigin& o, const ThreadVox<V>& tv,
+                                            const float* slot, int (&mn)[3], int (&mx)[3]) {
+    tile_bounds_pos<DP, V, IT>(g, o, tv, TilePos<kThreads * V, false>{slot, nullptr, 0, 0}, mn, mx);
 }
 
 // The patch contraction of contract() (pp_voxel.cuh) with the z loop rolled:
@@ -880,7 +911,8 @@ __device__ __forceinline__ void pull_voxel_lean(const LaunchArgs& a, int b, long
 
 // push_voxel_global (pp_voxel.cuh) for plain push, inlined with the z loop
 // rolled (weights and offsets rotate through slot 0) so that the fallback of the
-// batched kernel pins no registers across a call.
+// batched kernel pins no registers across a call.  The values are read with
+// plain loads: the batched kernel wrote them earlier in the same launch.
 template <int DP, typename IT>
 __device__ __forceinline__ void push_voxel_lean(const LaunchArgs& a, int b, long long v, float x0, float x1,
                                                 float x2) {
@@ -890,7 +922,7 @@ __device__ __forceinline__ void push_voxel_lean(const LaunchArgs& a, int b, long
     const IT sz = (IT)(g.d0[0] * g.d0[1]);
 #pragma unroll 1
     for (int c = 0; c < g.nc; ++c) {
-        const float v0 = __ldg(a.in + ((long long)b * g.nc + c) * n1 + v);
+        const float v0 = a.in[((long long)b * g.nc + c) * n1 + v];
         if (!finitef(v0)) continue;
         int b0, b1, b2;
         bnd_code(a, c, b0, b1, b2);
@@ -1270,11 +1302,13 @@ __device__ __forceinline__ void warp_scatter_tile(const float* rx, const float* 
 // channel-0 values kStages tiles ahead; the tile scatters into the shared
 // accumulator and flushes it with global reductions.  The flush clears every
 // element it reads, so the accumulator is zero again for the next tile.
-template <int DP, int OP, int V, typename IT, bool TMA>
+// AFF: the affine push -- positions A * (i, j, k, 1) from `aff`, no deformation.
+template <int DP, int OP, int V, typename IT, bool TMA, bool AFF = false>
 __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constant__ LaunchArgs a,
                                                             const __grid_constant__ TileGrid t,
                                                             const __grid_constant__ CUtensorMap phimap,
-                                                            const __grid_constant__ CUtensorMap valmap) {
+                                                            const __grid_constant__ CUtensorMap valmap,
+                                                            const __grid_constant__ AffineMap aff) {
     extern __shared__ __align__(128) float4 smem4[];
     constexpr int ORD = OP == kPushGrad ? 1 : 0;
     constexpr int NCOMP = OP == kPushGrad ? 3 : 1;
@@ -1321,7 +1355,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
     }
     __syncthreads();
     for (int j = 0; j < kStages && j < ntl; ++j)
-        ring_fill<V, NCOMP, TMA, IT>(ring, j, T0 + j * G, a, t, tv, phimap, valmap, a.in);
+        ring_fill<V, NCOMP, TMA, IT, AFF>(ring, j, T0 + j * G, a, t, tv, phimap, valmap, a.in);
     if (!TMA) __syncthreads();
 
     const unsigned acc_base = smem_addr(accf);
@@ -1329,16 +1363,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
         const TileOrigin o = tile_origin(t, T0 + j * G);
         const float* slot = ring.base + (j % kStages) * ring.slot_floats;
         if (!ring_wait<TMA>(ring, j)) s_abort = 1;
+        const TilePos<NV, AFF> pos{slot, &aff, t.lx, t.ly};
         // deformation validity, first-tap bounds and the channel-0 scale bound
         int mn[3], mx[3];
-        tile_bounds<DP, V, IT>(g, o, tv, slot, mn, mx);
+        tile_bounds_pos<DP, V, IT>(g, o, tv, pos, mn, mx);
         float bound0 = 0.f;
 #pragma unroll
         for (int q = 0; q < V; ++q) {
             const int lin = threadIdx.x + q * kThreads;
             float x0, x1, x2;
             if (tv.template index<IT>(o, q) < 0 ||
-                !load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2))
+                !pos(g, o, lin, x0, x1, x2))
                 continue;
             bool fin = true;
             float s1 = 0.f;
@@ -1358,7 +1393,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
                 const IT v = tv.template index<IT>(o, q);
                 const int lin = threadIdx.x + q * kThreads;
                 float x0, x1, x2;
-                if (v >= 0 && load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2))
+                if (v >= 0 && pos(g, o, lin, x0, x1, x2))
                     push_tile_fallback<DP, OP, IT>(a, o.b, (long long)v, x0, x1, x2);
             }
         } else if (box.mode == 1) {
@@ -1366,6 +1401,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
             int* acc_hi = reinterpret_cast<int*>(accf);
             int* acc_lo = acc_hi + box.size;
             const float* inb = a.in + (long long)o.b * g.nc * NCOMP * n1;
+            // the box geometry in registers: the scatter's reductions are memory
+            // barriers to the compiler, which would reload it from shared memory
+            const int bxo = box.xo, by0 = box.lo[1], bz0 = box.lo[2], bP = box.P, bQ = box.Q;
             for (int c = 0; c < g.nc; ++c) {
                 int b0, b1, b2;
                 bnd_code(a, c, b0, b1, b2);
@@ -1378,7 +1416,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
                         const IT v = tv.template index<IT>(o, q);
                         const int lin = threadIdx.x + q * kThreads;
                         float x0, x1, x2;
-                        if (v < 0 || !load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2))
+                        if (v < 0 || !pos(g, o, lin, x0, x1, x2))
                             continue;
                         bool fin = true;
                         float s1 = 0.f;
@@ -1409,7 +1447,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
                     const IT v = tv.template index<IT>(o, q);
                     const int lin = threadIdx.x + q * kThreads;
                     float x0, x1, x2;
-                    if (v < 0 || !load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2)) continue;
+                    if (v < 0 || !pos(g, o, lin, x0, x1, x2)) continue;
                     float val[NCOMP];
                     bool fin = true;
 #pragma unroll
@@ -1419,11 +1457,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
                     }
                     if (!fin) continue;
                     W3<DP, ORD> wx, wy, wz;
-                    const int ox = spline_taps32<DP, ORD>(x0, wx.w, wx.dw, wx.hw) - box.xo;
-                    const int oy = spline_taps32<DP, ORD>(x1, wy.w, wy.dw, wy.hw) - box.lo[1];
-                    const int oz = spline_taps32<DP, ORD>(x2, wz.w, wz.dw, wz.hw) - box.lo[2];
-                    const unsigned P4 = 4u * box.P, Q4 = 4u * box.Q;
-                    const unsigned base = acc_base + 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
+                    const int ox = spline_taps32<DP, ORD>(x0, wx.w, wx.dw, wx.hw) - bxo;
+                    const int oy = spline_taps32<DP, ORD>(x1, wy.w, wy.dw, wy.hw) - by0;
+                    const int oz = spline_taps32<DP, ORD>(x2, wz.w, wz.dw, wz.hw) - bz0;
+                    const unsigned P4 = 4u * bP, Q4 = 4u * bQ;
+                    const unsigned base = acc_base + 4u * (unsigned)(oz * bQ + oy * bP + ox);
                     const float sc = fixed ? fs.inv_q1 : 1.f;
                     const float w0 = val[0] * sc;
                     const float w1 = NCOMP > 1 ? val[NCOMP > 1 ? 1 : 0] * sc : 0.f;
@@ -1442,28 +1480,31 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
                         const int lin = threadIdx.x + q * kThreads;
                         int base = -1;
                         float x0, x1, x2;
-                        if (v >= 0 && load_valid(slot[lin], slot[NV + lin], slot[2 * NV + lin], g, x0, x1, x2)) {
+                        if (v >= 0 && pos(g, o, lin, x0, x1, x2)) {
                             const float val = c == 0 ? slot[3 * NV + lin] : __ldg(inb + (long long)c * n1 + v);
                             if (finitef(val)) {
                                 W3<DP, 0> wx, wy, wz;
-                                const int ox = spline_taps32<DP, 0>(x0, wx.w, wx.dw, wx.hw) - box.xo;
-                                const int oy = spline_taps32<DP, 0>(x1, wy.w, wy.dw, wy.hw) - box.lo[1];
-                                const int oz = spline_taps32<DP, 0>(x2, wz.w, wz.dw, wz.hw) - box.lo[2];
-                                base = oz * box.Q + oy * box.P + ox;
+                                const int ox = spline_taps32<DP, 0>(x0, wx.w, wx.dw, wx.hw) - bxo;
+                                const int oy = spline_taps32<DP, 0>(x1, wy.w, wy.dw, wy.hw) - by0;
+                                const int oz = spline_taps32<DP, 0>(x2, wz.w, wz.dw, wz.hw) - bz0;
+                                base = oz * bQ + oy * bP + ox;
                                 const float sv = val * sc;
-#pragma unroll
-                                for (int i = 0; i < DP; ++i) {
-                                    rx[lin * DPP + i] = wx.w[i];
-                                    ry[lin * DPP + i] = wy.w[i] * sv;
-                                    rz[lin * DPP + i] = wz.w[i];
-                                }
+                                // one 16-byte store per axis (DPP = 4; unused taps 0)
+                                auto w4 = [&](const float (&w)[DP], float m) {
+                                    return make_float4(w[0] * m, DP > 1 ? w[DP > 1 ? 1 : 0] * m : 0.f,
+                                                       DP > 2 ? w[DP > 2 ? 2 : 0] * m : 0.f,
+                                                       DP > 3 ? w[DP > 3 ? 3 : 0] * m : 0.f);
+                                };
+                                reinterpret_cast<float4*>(rx)[lin] = w4(wx.w, 1.f);
+                                reinterpret_cast<float4*>(ry)[lin] = w4(wy.w, sv);
+                                reinterpret_cast<float4*>(rz)[lin] = w4(wz.w, 1.f);
                             }
                         }
                         rb[lin] = base;
                     }
                     __syncthreads();   // records complete
                     // ... then every warp scatters whole voxels, one tap per lane
-                    warp_scatter_tile<DP, DPP, NV>(rx, ry, rz, rb, box.P, box.Q, acc_base, lo_off, fixed);
+                    warp_scatter_tile<DP, DPP, NV>(rx, ry, rz, rb, bP, bQ, acc_base, lo_off, fixed);
                 } else {
                     thread_scatter();
                 }
@@ -1485,12 +1526,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
         if constexpr (WSC) {
             if (box.mode == 1 && box.wsc) {   // the records sat in the accumulator budget: clear them
                 __syncthreads();
-                for (int i = threadIdx.x; i < kRec; i += kThreads) rx[i] = 0.f;
+                for (int i = threadIdx.x; i < kRec / 4; i += kThreads)
+                    reinterpret_cast<float4*>(rx)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
         }
         __syncthreads();   // ring slot j is free and the accumulator is clear
         if (j + kStages < ntl)
-            ring_fill<V, NCOMP, TMA, IT>(ring, j + kStages, T0 + (j + kStages) * G, a, t, tv, phimap, valmap, a.in);
+            ring_fill<V, NCOMP, TMA, IT, AFF>(ring, j + kStages, T0 + (j + kStages) * G, a, t, tv, phimap, valmap,
+                                              a.in);
         if (!TMA) __syncthreads();
     }
 }
@@ -1905,6 +1948,62 @@ __device__ __forceinline__ void batch_tile(const BatchItem& it, int lt, float* s
     }
 }
 
+// A tile of an item with per-dimension degrees: every voxel from global memory
+// (runtime degree per axis), each channel pulled and its value pushed straight
+// back with global atomics.
+__device__ __noinline__ void batch_tile_any(const BatchItem& it, int lt) {
+    constexpr int V = 2;
+    const LaunchArgs& a = it.pull;
+    const Geometry& g = a.g;
+    const long long n1 = g.n1;
+    const TileGrid& t = it.t;
+    const ThreadVox<V> tv(t, g);
+    const TileOrigin o = tile_origin(t, lt);
+    const int sy = (int)g.d0[0], sz = (int)(g.d0[0] * g.d0[1]);
+#pragma unroll 1
+    for (int q = 0; q < V; ++q) {
+        const int v = tv.template index<int>(o, q);
+        if (v < 0) continue;
+        const float* phi = a.phi + v;
+        float x0, x1, x2;
+        if (!load_valid(__ldg(phi), __ldg(phi + n1), __ldg(phi + 2 * n1), g, x0, x1, x2)) {
+            pull_voxel_nan<kPull>(a, 0, v);
+            continue;
+        }
+        Axis<0, 0, int> ax, ay, az;
+        constexpr int N = Axis<0, 0, int>::N;
+        int prev = -1;
+#pragma unroll 1
+        for (int c = 0; c < g.nc; ++c) {
+            int b0, b1, b2;
+            const int code = bnd_code(a, c, b0, b1, b2);
+            if (code != prev) {
+                ax.setup(x0, g.dp[0], b0, g.d0[0], 1);
+                ay.setup(x1, g.dp[1], b1, g.d0[1], sy);
+                az.setup(x2, g.dp[2], b2, g.d0[2], sz);
+                prev = code;
+            }
+            const float* f0 = a.in + (long long)c * g.n0;
+            float r[6];
+            contract<kPull, N>(ax, ay, az, ax.n, ay.n, az.n, true,
+                               [&](int k, int j, int i) { return __ldg(f0 + (az.off[k] + ay.off[j] + ax.off[i])); }, r);
+            a.out[(long long)c * n1 + v] = r[0];
+            if (!finitef(r[0])) continue;
+            float* out = it.push.out + (long long)c * g.n0;
+#pragma unroll 1
+            for (int k = 0; k < az.n; ++k) {
+#pragma unroll 1
+                for (int j = 0; j < ay.n; ++j) {
+                    const float cb = r[0] * (ay.w[j] * az.w[k]);
+                    float* row = out + (az.off[k] + ay.off[j]);
+#pragma unroll 1
+                    for (int i = 0; i < ax.n; ++i) atomicAdd(row + ax.off[i], cb * ax.w[i]);
+                }
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchItem* __restrict__ items, int nitems, int total,
                                                        unsigned* counter, int cap) {
     extern __shared__ __align__(128) float4 smem4[];
@@ -1931,6 +2030,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchItem* __restri
         const BatchItem& it = items[lo];
         const int lt = T - it.tile_begin;
         switch (it.dp) {
+            case 0: batch_tile_any(it, lt); break;
             case 1: batch_tile<1>(it, lt, sm, cap, box, red, sred); break;
             case 2: batch_tile<2>(it, lt, sm, cap, box, red, sred); break;
             case 3: batch_tile<3>(it, lt, sm, cap, box, red, sred); break;
@@ -2061,21 +2161,23 @@ cudaError_t launch_persistent(K kern, const TileGrid& t, size_t smem, cudaStream
     return cudaGetLastError();
 }
 
-template <int DP, int OP, int V, typename IT, bool PUSH>
-cudaError_t launch_v(const LaunchArgs& a, const TileGrid& t, cudaStream_t s) {
+// AFF (push only): the affine push, positions from `aff` instead of a.phi.
+template <int DP, int OP, int V, typename IT, bool PUSH, bool AFF = false>
+cudaError_t launch_v(const LaunchArgs& a, const TileGrid& t, cudaStream_t s, const AffineMap& aff = AffineMap{}) {
     constexpr int NV = kThreads * V;
     CUtensorMap phimap, valmap;
     std::memset(&phimap, 0, sizeof phimap);
     std::memset(&valmap, 0, sizeof valmap);
     const long long nb = a.g.nb, nc = a.g.nc;
-    bool tma = encode_tile_map(&phimap, a.phi, a.g.d1, 3 * nb, t, 3);
+    bool tma = AFF || encode_tile_map(&phimap, a.phi, a.g.d1, 3 * nb, t, 3);
     if constexpr (PUSH) {
         constexpr int NCOMP = OP == kPushGrad ? 3 : 1;
         tma = tma && encode_tile_map(&valmap, a.in, a.g.d1, NCOMP * nc * nb, t, NCOMP);
         const size_t smem = (size_t)kStages * (3 + NCOMP) * NV * 4 + (size_t)t.cap * 4 + 8 * kStages;
-        if (tma) return launch_persistent(k_push_tiled<DP, OP, V, IT, true>, t, smem, s, a, t, phimap, valmap);
-        return launch_persistent(k_push_tiled<DP, OP, V, IT, false>, t, smem, s, a, t, phimap, valmap);
+        if (tma) return launch_persistent(k_push_tiled<DP, OP, V, IT, true, AFF>, t, smem, s, a, t, phimap, valmap, aff);
+        return launch_persistent(k_push_tiled<DP, OP, V, IT, false, AFF>, t, smem, s, a, t, phimap, valmap, aff);
     } else {
+        static_assert(!AFF, "affine pull runs on the warp-specialised kernels");
         // interior boxes as one TMA copy of a fixed window when the tile is 8 wide
         // (the window's row pitch is bank-conflict free for 8-wide warp tiles)
         CUtensorMap imgmap;
@@ -2119,22 +2221,22 @@ cudaError_t launch_fused_dp(const LaunchArgs& a, const TileCfg& c, cudaStream_t 
     return launch_fused_v<DP, 1, IT>(a, t, s, grid);
 }
 
-template <int DP, int OP, typename IT, bool PUSH>
-cudaError_t launch_one(const LaunchArgs& a, const TileCfg& c, cudaStream_t s) {
+template <int DP, int OP, typename IT, bool PUSH, bool AFF = false>
+cudaError_t launch_one(const LaunchArgs& a, const TileCfg& c, cudaStream_t s, const AffineMap& aff) {
     const TileGrid t = make_grid(a, c);
     const int vox = 1 << (c.lx + c.ly + c.lz);
-    if (vox > kThreads) return launch_v<DP, OP, 2, IT, PUSH>(a, t, s);
-    return launch_v<DP, OP, 1, IT, PUSH>(a, t, s);
+    if (vox > kThreads) return launch_v<DP, OP, 2, IT, PUSH, AFF>(a, t, s, aff);
+    return launch_v<DP, OP, 1, IT, PUSH, AFF>(a, t, s, aff);
 }
 
-template <int OP, typename IT, bool PUSH>
-cudaError_t dispatch(const LaunchArgs& a, const TileCfg& t, cudaStream_t s) {
+template <int OP, typename IT, bool PUSH, bool AFF = false>
+cudaError_t dispatch(const LaunchArgs& a, const TileCfg& t, cudaStream_t s, const AffineMap& aff = AffineMap{}) {
     switch (a.g.dp[0]) {
-        case 1: return launch_one<1, OP, IT, PUSH>(a, t, s);
-        case 2: return launch_one<2, OP, IT, PUSH>(a, t, s);
-        case 3: return launch_one<3, OP, IT, PUSH>(a, t, s);
-        case 4: return launch_one<4, OP, IT, PUSH>(a, t, s);
-        default: return launch_one<5, OP, IT, PUSH>(a, t, s);
+        case 1: return launch_one<1, OP, IT, PUSH, AFF>(a, t, s, aff);
+        case 2: return launch_one<2, OP, IT, PUSH, AFF>(a, t, s, aff);
+        case 3: return launch_one<3, OP, IT, PUSH, AFF>(a, t, s, aff);
+        case 4: return launch_one<4, OP, IT, PUSH, AFF>(a, t, s, aff);
+        default: return launch_one<5, OP, IT, PUSH, AFF>(a, t, s, aff);
     }
 }
 

@@ -68,10 +68,29 @@ __device__ __forceinline__ TileOrigin ws_origin(const TileGrid& t, int T) {
     return r;
 }
 
-// First-tap bounds of one consumer thread's voxels of the tile in `slot`,
-// reduced over its warp (every lane ends with the warp's bounds).
-template <int DP, typename IT>
-__device__ __forceinline__ void ws_warp_bounds(const Geometry& g, const TileOrigin& o, const float* slot, int ctid,
+// Sample positions of a tile's voxels: x = phi - 1 from the tile's ring slot,
+// or (AFF, the affine ops) A * (i, j, k, 1) from the voxel's grid coordinates;
+// either way with the validity test.
+template <bool AFF>
+struct WsPos {
+    const float* slot;
+    const AffineMap* A;
+    __device__ __forceinline__ bool operator()(const Geometry& g, const TileOrigin& o, int lin, float& x0, float& x1,
+                                               float& x2) const {
+        if constexpr (AFF) {
+            affine_position(*A, (float)(o.x0 + (lin & 7)), (float)(o.y0 + ((lin >> 3) & 7)), (float)(o.z0 + (lin >> 6)),
+                            x0, x1, x2);
+            return position_valid(x0, x1, x2, g);
+        } else {
+            return load_valid(slot[lin], slot[kWsNV + lin], slot[2 * kWsNV + lin], g, x0, x1, x2);
+        }
+    }
+};
+
+// First-tap bounds of one consumer thread's voxels of the tile, reduced over
+// its warp (every lane ends with the warp's bounds).
+template <int DP, typename IT, class POS>
+__device__ __forceinline__ void ws_warp_bounds(const Geometry& g, const TileOrigin& o, const POS& pos, int ctid,
                                                int D0, int D1, int D2, int (&mn)[3], int (&mx)[3]) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -83,7 +102,7 @@ __device__ __forceinline__ void ws_warp_bounds(const Geometry& g, const TileOrig
         const int i = ctid + q * kWsCons;
         if (ws_index<IT>(o, i, D0, D1, D2) < 0) continue;
         float x[3];
-        if (!load_valid(slot[i], slot[kWsNV + i], slot[2 * kWsNV + i], g, x[0], x[1], x[2])) continue;
+        if (!pos(g, o, i, x[0], x[1], x[2])) continue;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const int f = first_tap32(x[k], DP);
@@ -308,8 +327,8 @@ __device__ __forceinline__ void ws_mirror_fixup(const Box& box, const Geometry& 
 // One consumer thread, one (tile, channel) unit of the pull family: its two
 // voxels against the staged box (dot ops accumulate into acc and store after
 // the last channel).
-template <int DP, int OP_, typename IT>
-__device__ __forceinline__ void ws_pull_unit(const LaunchArgs& a, const TileOrigin& o, int ctid, const float* slot,
+template <int DP, int OP_, typename IT, class POS>
+__device__ __forceinline__ void ws_pull_unit(const LaunchArgs& a, const TileOrigin& o, int ctid, const POS& pos,
                                              int c, const Box& box, const float* sm, float (&acc)[kWsV][3], int D0,
                                              int D1, int D2) {
     constexpr int OP = pull_base_op<OP_>();
@@ -323,7 +342,7 @@ __device__ __forceinline__ void ws_pull_unit(const LaunchArgs& a, const TileOrig
         const IT v = ws_index<IT>(o, lin, D0, D1, D2);
         if (v < 0) return;
         float x0, x1, x2;
-        if (!load_valid(slot[lin], slot[kWsNV + lin], slot[2 * kWsNV + lin], g, x0, x1, x2)) {
+        if (!pos(g, o, lin, x0, x1, x2)) {
             if (!pull_is_dot<OP_>() || last) {
                 float* out = pull_out<OP_>(a, o.b, c, (long long)v);
 #pragma unroll
@@ -365,11 +384,13 @@ __device__ __forceinline__ void ws_pull_unit(const LaunchArgs& a, const TileOrig
     }
 }
 
-template <int DP, int OP, typename IT>
+// AFF: the affine pull -- no deformation ring; positions from `aff`.
+template <int DP, int OP, typename IT, bool AFF>
 __global__ void __launch_bounds__(kWsThreads, 1) k_pull_ws(const __grid_constant__ LaunchArgs a,
                                                            const __grid_constant__ TileGrid t,
                                                            const __grid_constant__ CUtensorMap phimap,
-                                                           const __grid_constant__ CUtensorMap imgmap) {
+                                                           const __grid_constant__ CUtensorMap imgmap,
+                                                           const __grid_constant__ AffineMap aff) {
     extern __shared__ __align__(128) float4 smem4[];
     __shared__ __align__(8) unsigned long long bars[kWsStages + 2 * kWsBufs + 2];
     __shared__ Box rec[kWsBufs];
@@ -405,7 +426,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_pull_ws(const __grid_constant
     if (warp == kWsCons / 32) {
         // ---------------- producer warp ----------------
         auto load_phi = [&](int j) {   // lane 0: tile j's deformation into slot j % kWsStages
-            if (lane == 0) {
+            if (!AFF && lane == 0) {
                 const TileOrigin o = ws_origin(t, T0 + j * G);
                 const unsigned bar = phi_full + 8u * (j % kWsStages);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -469,10 +490,10 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_pull_ws(const __grid_constant
     const int ctid = threadIdx.x;
     auto publish_bounds = [&](int j) -> bool {
         const TileOrigin o = ws_origin(t, T0 + j * G);
-        const float* slot = ring + (j % kWsStages) * 3 * kWsNV;
-        if (!mbar_wait(phi_full + 8u * (j % kWsStages), (unsigned)((j / kWsStages) & 1))) return false;
+        const WsPos<AFF> pos{ring + (j % kWsStages) * 3 * kWsNV, &aff};
+        if (!AFF && !mbar_wait(phi_full + 8u * (j % kWsStages), (unsigned)((j / kWsStages) & 1))) return false;
         int mn[3], mx[3];
-        ws_warp_bounds<DP, IT>(g, o, slot, ctid, D0, D1, D2, mn, mx);
+        ws_warp_bounds<DP, IT>(g, o, pos, ctid, D0, D1, D2, mn, mx);
         if (lane == 0) {
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
@@ -486,7 +507,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_pull_ws(const __grid_constant
     if (!publish_bounds(0)) s_abort = 1;
     for (int j = 0; j < ntl && !s_abort; ++j) {
         const TileOrigin o = ws_origin(t, T0 + j * G);
-        const float* slot = ring + (j % kWsStages) * 3 * kWsNV;
+        const WsPos<AFF> pos{ring + (j % kWsStages) * 3 * kWsNV, &aff};
         if (j + 1 < ntl && !publish_bounds(j + 1)) s_abort = 1;
         if (s_abort) break;
         float acc[kWsV][3];
@@ -509,7 +530,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_pull_ws(const __grid_constant
                     asm volatile("bar.sync 1, %0;" ::"n"(kWsCons) : "memory");
                 }
             }
-            ws_pull_unit<DP, OP, IT>(a, o, ctid, slot, c, box, buf, acc, D0, D1, D2);
+            ws_pull_unit<DP, OP, IT>(a, o, ctid, pos, c, box, buf, acc, D0, D1, D2);
             __syncwarp();
             if (lane == 0) mbar_arrive(box_empty + 8u * b);
         }
@@ -585,17 +606,18 @@ bool encode_window_map(CUtensorMap* map, const float* base, const long long d[3]
     return r == CUDA_SUCCESS;
 }
 
-template <int DP, int OP, typename IT>
-cudaError_t launch_ws_one(const LaunchArgs& a, const TileGrid& t, const CUtensorMap& phimap, cudaStream_t s) {
+template <int DP, int OP, typename IT, bool AFF>
+cudaError_t launch_ws_one(const LaunchArgs& a, const TileGrid& t, const CUtensorMap& phimap, const AffineMap& aff,
+                          cudaStream_t s) {
     CUtensorMap imgmap;
     std::memset(&imgmap, 0, sizeof imgmap);
     TileGrid tt = t;
     tt.img_tma = encode_window_map(&imgmap, a.in, a.g.d0, (long long)a.g.nc * a.g.nb) ? 1 : 0;
-    auto kern = k_pull_ws<DP, OP, IT>;
+    auto kern = k_pull_ws<DP, OP, IT, AFF>;
     cudaError_t e = opt_in(kern, kWsSmem);
     if (e != cudaSuccess) return e;
     const int grid = tt.ntiles < sm_count() ? tt.ntiles : sm_count();
-    kern<<<grid, kWsThreads, kWsSmem, s>>>(a, tt, phimap, imgmap);
+    kern<<<grid, kWsThreads, kWsSmem, s>>>(a, tt, phimap, imgmap, aff);
     return cudaGetLastError();
 }
 

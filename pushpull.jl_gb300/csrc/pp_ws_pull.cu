@@ -4,14 +4,15 @@
 namespace pp {
 
 namespace {
-template <int OP, typename IT>
-cudaError_t ws_dispatch(const LaunchArgs& a, const TileGrid& t, const CUtensorMap& phimap, cudaStream_t s) {
+template <int OP, typename IT, bool AFF = false>
+cudaError_t ws_dispatch(const LaunchArgs& a, const TileGrid& t, const CUtensorMap& phimap, cudaStream_t s,
+                        const AffineMap& aff = AffineMap{}) {
     switch (a.g.dp[0]) {
-        case 1: return launch_ws_one<1, OP, IT>(a, t, phimap, s);
-        case 2: return launch_ws_one<2, OP, IT>(a, t, phimap, s);
-        case 3: return launch_ws_one<3, OP, IT>(a, t, phimap, s);
-        case 4: return launch_ws_one<4, OP, IT>(a, t, phimap, s);
-        default: return launch_ws_one<5, OP, IT>(a, t, phimap, s);
+        case 1: return launch_ws_one<1, OP, IT, AFF>(a, t, phimap, aff, s);
+        case 2: return launch_ws_one<2, OP, IT, AFF>(a, t, phimap, aff, s);
+        case 3: return launch_ws_one<3, OP, IT, AFF>(a, t, phimap, aff, s);
+        case 4: return launch_ws_one<4, OP, IT, AFF>(a, t, phimap, aff, s);
+        default: return launch_ws_one<5, OP, IT, AFF>(a, t, phimap, aff, s);
     }
 }
 }  // namespace
@@ -39,6 +40,15 @@ cudaError_t launch_ws_pull(int op, const LaunchArgs& a, cudaStream_t s) {
     if (op == kPullGrad)
         return small ? ws_dispatch<kPullGrad, int>(a, t, phimap, s) : ws_dispatch<kPullGrad, long long>(a, t, phimap, s);
     return cudaErrorNotSupported;
+}
+
+// Affine pull (pp_pull_affine) on the same kernels, positions computed in place.
+cudaError_t launch_ws_pull_affine(const LaunchArgs& a, const AffineMap& A, cudaStream_t s) {
+    const TileGrid t = ws_make_grid(a);
+    CUtensorMap none;
+    std::memset(&none, 0, sizeof none);
+    const bool small = a.g.n0 < (1LL << 31) - 1 && a.g.n1 < (1LL << 31) - 1;
+    return small ? ws_dispatch<kPull, int, true>(a, t, none, s, A) : ws_dispatch<kPull, long long, true>(a, t, none, s, A);
 }
 
 unsigned status_ws_pull(bool reset) { return unit_status(reset); }

@@ -103,6 +103,24 @@ def config5(seed: int = 5) -> Workload:
                     deformation(d, seed + 1, 12.0, 3.0, contraction=0.25), (3, 3, 3), 1, 1, {})
 
 
+def affine_map(d, seed: int = 6) -> np.ndarray:
+    """1-based 4x4 affine of a d grid onto itself: rotations of up to 10 degrees
+    about each axis and scalings in [0.9, 1.1] about the centre, plus a shift of
+    up to 3 voxels (a rigid-plus-zoom registration update)."""
+    rng = np.random.default_rng(seed)
+    th = rng.uniform(-np.pi / 18, np.pi / 18, 3)
+    c, s = np.cos(th), np.sin(th)
+    R = (np.array([[1, 0, 0], [0, c[0], -s[0]], [0, s[0], c[0]]])
+         @ np.array([[c[1], 0, s[1]], [0, 1, 0], [-s[1], 0, c[1]]])
+         @ np.array([[c[2], -s[2], 0], [s[2], c[2], 0], [0, 0, 1]]))
+    M = R @ np.diag(rng.uniform(0.9, 1.1, 3))
+    ctr = 0.5 * (np.array(d, dtype=np.float64) + 1)
+    A = np.eye(4, dtype=np.float32)
+    A[:3, :3] = M
+    A[:3, 3] = ctr - M @ ctr + rng.uniform(-3, 3, 3)
+    return A
+
+
 def batched_pairs(seed: int = 4, npairs: int = 32, levels: int = 3):
     """Uneven batch: sizes uniform in [64,256]x[64,256]x[64,192], 1-3 channels,
     degree from {1,2,3}; each pair with a pyramid of ``levels`` (each level halved)."""

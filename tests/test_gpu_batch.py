@@ -77,3 +77,33 @@ def test_batch_graph_replay(pkg):
         assert (it["out"] - ref).abs().max() <= 1e-4 * ref.abs().max()
     assert pkg.native_library().pp_device_status(1) == 0
     plan.close()
+
+
+def test_batch_general_items(pkg, O):
+    """Items with per-dimension degrees and per-channel boundary triples, mixed
+    with isotropic ones, in one plan: each against its single calls and the FP64
+    oracle."""
+    W = importlib.import_module("pushpull_gb300.workloads")
+    B = importlib.import_module("pushpull_gb300.batch")
+    L = pkg.layout
+    specs = [((30, 26, 22), 2, (1, 3, 2), [(0, 1, 2), (1, 1, 1)], 1),
+             ((24, 20, 28), 3, 3, [(1, 1, 1), (2, 2, 2), (0, 0, 0)], 1),
+             ((20, 18, 16), 1, (3, 0, 4), 1, 0),
+             ((32, 24, 16), 2, 2, (0, 1, 2), 1)]
+    items = _items(pkg, W, specs)
+    plan = B.BatchPlan(items, zero_outputs=True)
+    plan.run()
+    torch.cuda.synchronize()
+    assert pkg.native_library().pp_device_status(1) == 0
+    for it, (d, nc, deg, bnd, ext) in zip(items, specs):
+        s = it["sett"]
+        ref1 = pkg.pull(it["f0"], it["phi"], s)
+        ref0 = pkg.push(ref1, it["phi"], d, s)
+        assert torch.equal(torch.isnan(it["f1"]), torch.isnan(ref1))
+        assert rel_err(L.to_numpy(it["f1"]), L.to_numpy(ref1)) <= 1e-5
+        assert rel_err(L.to_numpy(it["out"]), L.to_numpy(ref0)) <= 1e-4
+        so = O.Sett.make(deg, bnd, ext)
+        f0, phi, f1 = L.to_numpy(it["f0"]), L.to_numpy(it["phi"]), L.to_numpy(it["f1"])
+        assert rel_err(f1, O.pull(f0, phi, so)) <= 1e-5
+        assert rel_err(L.to_numpy(it["out"]), O.push(f1, phi, d, so)) <= 1e-4
+    plan.close()
