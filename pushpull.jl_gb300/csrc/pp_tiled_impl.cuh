@@ -1223,11 +1223,20 @@ __device__ __forceinline__ void push_scatter(const WT& wx, const WT& wy, const W
     }
 }
 
-// Push ops and degrees that scatter one voxel per warp instruction: plain push
-// at DP = 3 and 4 (a degree-4 box would need pitches of 37 elements or more).
+// Push ops and degrees that scatter one voxel per warp instruction: push and
+// push_grad at DP = 3 and 4 (a degree-4 box would need pitches of 37 elements or
+// more).
 template <int DP, int OP>
 __host__ __device__ constexpr bool warp_scatter() {
-    return OP == kPush && (DP == 3 || DP == 4);
+    return DP == 3 || DP == 4;
+}
+
+// float4 record arrays per voxel of the warp-cooperative scatter: push keeps
+// x, y (times the scaled value) and z weights; push_grad keeps v0 dw_x, v1 w_x,
+// v2 w_x (values scaled), then w_y, dw_y, w_z, dw_z.
+template <int OP>
+__host__ __device__ constexpr int scatter_records() {
+    return OP == kPushGrad ? 7 : 3;
 }
 
 // Warp-cooperative scatter of a tile's recorded voxels into the fixed-point
@@ -1246,13 +1255,14 @@ __device__ __forceinline__ void red_f32_nb(unsigned a, float v) {
     asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(a), "f"(v));
 }
 
-template <int DP, int DPP, int NV>
-__device__ __forceinline__ void warp_scatter_tile(const float* rx, const float* ry, const float* rz, const int* rb,
-                                                  int P, int Q, unsigned acc_base, unsigned lo_off, bool fixed) {
+template <int DP, int OP, int DPP, int NV>
+__device__ __forceinline__ void warp_scatter_tile(const float* rec, const int* rb, int P, int Q, unsigned acc_base,
+                                                  unsigned lo_off, bool fixed) {
     constexpr int T = DP * DP * DP;
     constexpr int PASSES = (T + 31) / 32;
     constexpr int NW = kThreads / 32;
-    static_assert(NV % (2 * NW) == 0, "two voxels per warp iteration");
+    constexpr int U = OP == kPushGrad ? 1 : 2;   // voxels per warp iteration (registers)
+    static_assert(NV % (U * NW) == 0, "whole warp iterations");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int ti[PASSES], tj[PASSES], tk[PASSES], off[PASSES];
 #pragma unroll
@@ -1263,22 +1273,32 @@ __device__ __forceinline__ void warp_scatter_tile(const float* rx, const float* 
         tk[p] = tt / (DP * DP);
         off[p] = ti[p] + P * tj[p] + Q * tk[p];
     }
-    // two voxels per iteration: all record loads first, then the reductions
-    for (int s0 = warp; s0 < NV; s0 += 2 * NW) {
-        int bv[2];
-        float y[2][PASSES];
+    // U voxels per iteration: all record loads first, then the reductions
+    for (int s0 = warp; s0 < NV; s0 += U * NW) {
+        int bv[U];
+        float y[U][PASSES];
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
+        for (int u = 0; u < U; ++u) {
             const int sidx = s0 + u * NW;
             bv[u] = rb[sidx];
-            const float* X = rx + sidx * DPP;
-            const float* Y = ry + sidx * DPP;
-            const float* Z = rz + sidx * DPP;
+            const float* R = rec + sidx * DPP;   // record array r of this voxel at R + r * DPP * NV
+            constexpr int RS = DPP * NV;
+            if constexpr (OP == kPushGrad) {
+                // v0 dwx wy wz + v1 wx dwy wz + v2 wx wy dwz = wz (wy A + dwy B) + dwz (wy C)
 #pragma unroll
-            for (int p = 0; p < PASSES; ++p) y[u][p] = (X[ti[p]] * Y[tj[p]]) * Z[tk[p]];
+                for (int p = 0; p < PASSES; ++p) {
+                    const float A = R[ti[p]], B = R[RS + ti[p]], C = R[2 * RS + ti[p]];
+                    const float Y = R[3 * RS + tj[p]], DY = R[4 * RS + tj[p]];
+                    const float Z = R[5 * RS + tk[p]], DZ = R[6 * RS + tk[p]];
+                    y[u][p] = fmaf(Z, fmaf(Y, A, DY * B), DZ * (Y * C));
+                }
+            } else {
+#pragma unroll
+                for (int p = 0; p < PASSES; ++p) y[u][p] = (R[ti[p]] * R[RS + tj[p]]) * R[2 * RS + tk[p]];
+            }
         }
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
+        for (int u = 0; u < U; ++u) {
             if (bv[u] < 0) continue;   // warp-uniform: every lane read the same record
 #pragma unroll
             for (int p = 0; p < PASSES; ++p) {
@@ -1313,8 +1333,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
     constexpr int ORD = OP == kPushGrad ? 1 : 0;
     constexpr int NCOMP = OP == kPushGrad ? 3 : 1;
     constexpr int NV = kThreads * V;
-    // push at degrees 2 and 3 scatters one voxel per warp instruction (see
-    // kScatterQMask); other ops and degrees one voxel per thread
+    // contracted tiles of push and push_grad at degrees 2 and 3 scatter one voxel
+    // per warp instruction (see kScatterQMask); other tiles and degrees one voxel
+    // per thread
     constexpr bool WSC = warp_scatter<DP, OP>();
     constexpr int DPP = 4;   // record stride per axis (DP <= 4 under WSC)
     __shared__ int red[8][7];
@@ -1337,13 +1358,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
     float* accf = sm + kStages * (3 + NCOMP) * NV;
     ring.bars = smem_addr(accf + t.cap);
     // voxel records of the warp-cooperative scatter (contracted tiles only), at
-    // the top of the accumulator budget: x weights, y weights times the scaled
-    // value, z weights, and the box-relative first tap (-1: skip)
-    constexpr int kRec = (3 * DPP + 1) * NV;
+    // the top of the accumulator budget: the float4 arrays of scatter_records,
+    // then the box-relative first tap (-1: skip)
+    constexpr int NREC = scatter_records<OP>();
+    constexpr int kRec = (NREC * DPP + 1) * NV;
     float* rx = accf + (WSC ? t.cap - kRec : 0);
-    float* ry = rx + DPP * NV;
-    float* rz = ry + DPP * NV;
-    int* rb = reinterpret_cast<int*>(rz + DPP * NV);
+    int* rb = reinterpret_cast<int*>(rx + NREC * DPP * NV);
     for (int i = threadIdx.x; i < (t.cap >> 2); i += kThreads)
         reinterpret_cast<float4*>(accf)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (threadIdx.x == 0) {
@@ -1481,30 +1501,54 @@ __global__ void __launch_bounds__(kThreads, 2) k_push_tiled(const __grid_constan
                         int base = -1;
                         float x0, x1, x2;
                         if (v >= 0 && pos(g, o, lin, x0, x1, x2)) {
-                            const float val = c == 0 ? slot[3 * NV + lin] : __ldg(inb + (long long)c * n1 + v);
-                            if (finitef(val)) {
-                                W3<DP, 0> wx, wy, wz;
-                                const int ox = spline_taps32<DP, 0>(x0, wx.w, wx.dw, wx.hw) - bxo;
-                                const int oy = spline_taps32<DP, 0>(x1, wy.w, wy.dw, wy.hw) - by0;
-                                const int oz = spline_taps32<DP, 0>(x2, wz.w, wz.dw, wz.hw) - bz0;
-                                base = oz * bQ + oy * bP + ox;
-                                const float sv = val * sc;
-                                // one 16-byte store per axis (DPP = 4; unused taps 0)
-                                auto w4 = [&](const float (&w)[DP], float m) {
+                            float val[NCOMP];
+                            bool fin = true;
+#pragma unroll
+                            for (int p = 0; p < NCOMP; ++p) {
+                                val[p] = c == 0 ? slot[(3 + p) * NV + lin]
+                                                : __ldg(inb + (long long)c * NCOMP * n1 + v + p * n1);
+                                fin = fin && finitef(val[p]);
+                            }
+                            if (fin) {
+                                // one 16-byte store per record array (DPP = 4; unused taps 0),
+                                // one axis at a time
+                                auto w4 = [&](const float* w, float m) {
                                     return make_float4(w[0] * m, DP > 1 ? w[DP > 1 ? 1 : 0] * m : 0.f,
                                                        DP > 2 ? w[DP > 2 ? 2 : 0] * m : 0.f,
                                                        DP > 3 ? w[DP > 3 ? 3 : 0] * m : 0.f);
                                 };
-                                reinterpret_cast<float4*>(rx)[lin] = w4(wx.w, 1.f);
-                                reinterpret_cast<float4*>(ry)[lin] = w4(wy.w, sv);
-                                reinterpret_cast<float4*>(rz)[lin] = w4(wz.w, 1.f);
+                                float4* R4 = reinterpret_cast<float4*>(rx) + lin;
+                                W3<DP, ORD> wa;
+                                const int ox = spline_taps32<DP, ORD>(x0, wa.w, wa.dw, wa.hw) - bxo;
+                                if constexpr (OP == kPushGrad) {
+                                    R4[0] = w4(wa.dw, val[0] * sc);
+                                    R4[NV] = w4(wa.w, val[NCOMP > 1 ? 1 : 0] * sc);
+                                    R4[2 * NV] = w4(wa.w, val[NCOMP > 2 ? 2 : 0] * sc);
+                                } else {
+                                    R4[0] = w4(wa.w, 1.f);
+                                }
+                                const int oy = spline_taps32<DP, ORD>(x1, wa.w, wa.dw, wa.hw) - by0;
+                                if constexpr (OP == kPushGrad) {
+                                    R4[3 * NV] = w4(wa.w, 1.f);
+                                    R4[4 * NV] = w4(wa.dw, 1.f);
+                                } else {
+                                    R4[NV] = w4(wa.w, val[0] * sc);
+                                }
+                                const int oz = spline_taps32<DP, ORD>(x2, wa.w, wa.dw, wa.hw) - bz0;
+                                if constexpr (OP == kPushGrad) {
+                                    R4[5 * NV] = w4(wa.w, 1.f);
+                                    R4[6 * NV] = w4(wa.dw, 1.f);
+                                } else {
+                                    R4[2 * NV] = w4(wa.w, 1.f);
+                                }
+                                base = oz * bQ + oy * bP + ox;
                             }
                         }
                         rb[lin] = base;
                     }
                     __syncthreads();   // records complete
                     // ... then every warp scatters whole voxels, one tap per lane
-                    warp_scatter_tile<DP, DPP, NV>(rx, ry, rz, rb, bP, bQ, acc_base, lo_off, fixed);
+                    warp_scatter_tile<DP, OP, DPP, NV>(rx, rb, bP, bQ, acc_base, lo_off, fixed);
                 } else {
                     thread_scatter();
                 }
