@@ -272,7 +272,10 @@ def run_gpu(args):
         torch.cuda.synchronize()
         if i >= 3:
             pg_ms.append(e0.elapsed_time(e1))
-    del g1
+    # push_grad of that gradient field back through the same deformation
+    accg = L.empty(d0, device=dev)
+    pushg_ms = _timeit(lambda: pkg.push_grad(g1, phi, d0, s, out=accg, accumulate=False), max(args.steps, 5), flush)
+    del g1, accg
     # affine pull and push of the same image (positions A (i, j, k, 1) computed
     # in the kernels in place of a deformation), outside the timed step
     from pushpull_gb300 import workloads as W
@@ -372,15 +375,20 @@ def run_gpu(args):
     bytes_pg = 12 * n1 + 4 * nc * n0 + 12 * nc * n1
     kernels["pull_grad"] = {"ms": mg, "GB_s": bytes_pg / (mg * 1e-3) / 1e9,
                             "frac_of_peak": bytes_pg / (mg * 1e-3) / 1e9 / peak, "Gvox_s": n1 / (mg * 1e-3) / 1e9}
+    bytes_pushg = 12 * n1 + 12 * nc * n1 + 4 * nc * n0
+    kernels["push_grad"] = {"ms": pushg_ms, "GB_s": bytes_pushg / (pushg_ms * 1e-3) / 1e9,
+                            "frac_of_peak": bytes_pushg / (pushg_ms * 1e-3) / 1e9 / peak,
+                            "Gvox_s": n1 / (pushg_ms * 1e-3) / 1e9}
     bytes_aff = 4 * nc * n0 + 4 * nc * n1
     for k, ms in (("affine_pull", aff_pull_ms), ("affine_push", aff_push_ms)):
         kernels[k] = {"ms": ms, "GB_s": bytes_aff / (ms * 1e-3) / 1e9,
                       "frac_of_peak": bytes_aff / (ms * 1e-3) / 1e9 / peak, "Gvox_s": n1 / (ms * 1e-3) / 1e9}
     kernels["affine_map"] = [[float(v) for v in row] for row in Aff]
-    for k in ("pull", "push", "pull_grad", "affine_pull", "affine_push"):
+    for k in ("pull", "push", "pull_grad", "push_grad", "affine_pull", "affine_push"):
         kernels[k]["traffic_bytes_ncu"] = TRAFFIC.get(k)
     kernels["bytes_model"] = ("algorithmic bytes per launch: pull 12 n1 (phi) + 4 n0 (image, once) + 4 n1 (out); "
                               "push 12 n1 + 4 n1 (values) + 4 n0 (image written once); pull_grad 12 n1 + 4 n0 + 12 n1; "
+                              "push_grad 12 n1 + 12 n1 (gradient) + 4 n0; "
                               "affine pull 4 n0 + 4 n1, affine push 4 n1 + 4 n0 (no deformation)")
     cpu = None
     if not args.no_cpu and ws == 1 or (not args.no_cpu and rank == 0):

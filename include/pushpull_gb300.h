@@ -50,7 +50,7 @@ enum pp_status {
     PP_ERR_CHANNELS = 5,      /* nc/nb < 1 or nbnd not in {1, nc}                    */
     PP_ERR_ALIGN = 6,         /* float pointer not 4-byte aligned                    */
     PP_ERR_CUDA = 7,          /* a CUDA runtime call failed                          */
-    PP_ERR_UNSUPPORTED = 8,   /* request outside what this build supports            */
+    PP_ERR_UNSUPPORTED = 8,   /* request outside what this library supports          */
     PP_ERR_TOO_LARGE = 9,     /* request exceeds a fixed capacity                    */
     PP_ERR_TIMEOUT = 10       /* a bounded device-side wait gave up                  */
 };

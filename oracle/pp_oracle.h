@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  The shipped library never links or calls this
  * code.  Only the tests, the smoke check and the benchmark's CPU-baseline leg
- * load it, as the checker or as the timed CPU port.
+ * load it, as the parity reference or as the timed CPU port.
  *
  * Layout and arguments follow the reference C ABI (artifacts/C/pushpull.h:1-14):
  * one (batch, channel) slice per call, column-major volumes, the deformation
