@@ -78,7 +78,7 @@ def _oracle_threads():
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each kernel on this
 # workload, from one ncu capture each (profiles/k_pull_ws_192cubic.md, k_push_tiled_192cubic.md,
 # k_pull_ws_affine_192cubic.md, k_push_tiled_affine_192cubic.md)
-TRAFFIC = {"pull": 126_495_488, "push": 152_941_824, "affine_pull": 28_766_464, "affine_push": 56_648_448}
+TRAFFIC = {"pull": 125_749_248, "push": 152_941_824, "affine_pull": 28_637_184, "affine_push": 56_648_448}
 
 
 class Clocks:

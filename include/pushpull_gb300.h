@@ -234,7 +234,7 @@ enum pp_path { PP_PATH_AUTO = 0, PP_PATH_DIRECT = 1 };
  * degrees 0 and 1, where gathering straight from L2 beats staging a box.  The
  * code (lx, ly, lz) = (3, 3, 4) selects, for pull and pull_grad, the
  * warp-specialised kernels (one producer warp streams the deformation and
- * stages footprint boxes by TMA while fifteen consumer warps evaluate 8x8x15
+ * stages footprint boxes by TMA while fifteen consumer warps evaluate 8x8x30
  * tiles; their box budget is fixed); it is the default at degrees 2..4.  No
  * reference counterpart (the reference launches one thread per voxel with no
  * tiling, ext/pushpull_gpu.jl:386-391); used by the autotuner. */

@@ -95,7 +95,7 @@ bool g_tiles_init = false;
 int g_path = PP_PATH_AUTO;
 
 // The tile code (lx, ly, lz) = (3, 3, 4) selects the warp-specialised pull
-// kernels (pp_ws.cuh, 8 x 8 x 15 tiles); every other shape the
+// kernels (pp_ws.cuh, 8 x 8 x 30 tiles); every other shape the
 // block-synchronous ones.
 bool is_ws_tile(const TileCfg& t) { return t.lx == 3 && t.ly == 3 && t.lz == 4 && t.cap > 0; }
 
@@ -113,7 +113,7 @@ void init_tiles_locked() {
     // pull and pull_grad at degrees 2..4: the warp-specialised kernels
     // (192^3 cubic, GB300: pull 0.179 vs 0.254 ms, pull_grad 0.198 vs 0.262 ms)
     for (int op = 0; op < 2; ++op)
-        for (int d = 2; d < 5; ++d) g_tiles[op][d] = TileCfg{3, 3, 4, 9216};
+        for (int d = 2; d < 5; ++d) g_tiles[op][d] = TileCfg{3, 3, 4, 15360};
     g_tiles_init = true;
 }
 }  // namespace
@@ -479,7 +479,7 @@ int pp_autotune(int op, float* out, const float* phi, const float* in, const pp_
         const bool ws = t[0] == 3 && t[1] == 3 && t[2] == 4;
         if (ws && is_push) continue;
         for (int ci = 0; ci < (ws ? 1 : 3) && rc == PP_OK; ++ci) {
-            const int cap = ws ? 9216 : (is_push ? caps_push[ci] : caps_pull[ci]);
+            const int cap = ws ? 15360 : (is_push ? caps_push[ci] : caps_pull[ci]);
             if (pp_set_tile(op, deg[0], t[0], t[1], t[2], cap) != PP_OK) continue;
             if ((rc = measure(ms)) != PP_OK) break;
             if (ms < bestv) {

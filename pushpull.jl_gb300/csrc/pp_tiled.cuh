@@ -13,7 +13,7 @@ struct TileCfg {
 };
 
 bool tiled_supported(const LaunchArgs& a, const TileCfg& t);
-// warp-specialised pull family (8 x 8 x 15 tiles, pp_ws.cuh): geometry test and
+// warp-specialised pull family (8 x 8 x 30 tiles, pp_ws.cuh): geometry test and
 // launch (cudaErrorNotSupported for ops or layouts it does not take)
 bool ws_supported(const LaunchArgs& a);
 cudaError_t launch_ws_pull(int op, const LaunchArgs& a, cudaStream_t s);

@@ -3,14 +3,14 @@
 // Included after pp_tiled_impl.cuh (whose helpers it uses) by pp_ws_pull.cu.
 //
 // One CTA per SM: 15 consumer warps and one producer warp (512 threads, so
-// every thread keeps 128 registers).  The CTA walks tiles of 8 x 8 x 15 sample
+// every thread keeps 128 registers).  The CTA walks tiles of 8 x 8 x 30 sample
 // voxels, two per consumer thread, in (tile, channel) units:
 //   * the producer warp streams each tile's deformation into a ring of
 //     shared-memory slots with one TMA copy per tile (mbarrier complete_tx);
 //   * every consumer warp reduces the first taps of its own voxels of tile
 //     j + 1 before it evaluates tile j and publishes the warp's bounds;
 //   * the producer combines the fifteen records into the tile's footprint box
-//     and, for a box inside the image that fits a fixed 24 x 16 x 24 window,
+//     and, for a box inside the image that fits a fixed 24 x 16 x 40 window,
 //     stages it with one TMA copy into one of two buffers while the consumers
 //     still evaluate the previous unit; it then publishes the box record;
 //   * boundary boxes whose margins mirror (DCT-II, DST-II) onto elements of the
@@ -33,12 +33,12 @@ namespace {
 
 constexpr int kWsCons = 480;                   // consumer threads (15 warps)
 constexpr int kWsThreads = kWsCons + 32;       // plus the producer warp
-constexpr int kWsV = 2;                        // sample voxels per consumer thread
-constexpr int kWsTz = 15;                      // tile: 8 x 8 x 15 sample voxels
-constexpr int kWsNV = kWsCons * kWsV;          // 960 voxels per tile
-constexpr int kWsStages = 4;                   // deformation ring slots
+constexpr int kWsV = 4;                        // sample voxels per consumer thread
+constexpr int kWsTz = 30;                      // tile: 8 x 8 x 30 sample voxels
+constexpr int kWsNV = kWsCons * kWsV;          // 1920 voxels per tile
+constexpr int kWsStages = 3;                   // deformation ring slots
 constexpr int kWsBufs = 2;                     // box buffers
-constexpr int kWsWinX = 24, kWsWinY = 16, kWsWinZ = 24;   // TMA image window (row pitch 24)
+constexpr int kWsWinX = 24, kWsWinY = 16, kWsWinZ = 40;   // TMA image window (row pitch 24)
 constexpr int kWsCap = kWsWinX * kWsWinY * kWsWinZ;         // floats per box buffer
 constexpr size_t kWsSmem = (size_t)(kWsStages * 3 * kWsNV + kWsBufs * kWsCap) * sizeof(float);
 
@@ -46,7 +46,7 @@ __device__ __forceinline__ void mbar_arrive(unsigned bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-// Tile-local voxel lin (x fastest, 8 x 8 x 15) -> linear sample index, or -1.
+// Tile-local voxel lin (x fastest, 8 x 8 x 30) -> linear sample index, or -1.
 template <typename IT>
 __device__ __forceinline__ IT ws_index(const TileOrigin& o, int lin, int D0, int D1, int D2) {
     const int gx = o.x0 + (lin & 7), gy = o.y0 + ((lin >> 3) & 7), gz = o.z0 + (lin >> 6);
@@ -54,7 +54,7 @@ __device__ __forceinline__ IT ws_index(const TileOrigin& o, int lin, int D0, int
     return (IT)gx + (IT)D0 * ((IT)gy + (IT)D1 * (IT)gz);
 }
 
-// Origin of linear tile T (x fastest, batch slowest) of the 8 x 8 x 15 grid.
+// Origin of linear tile T (x fastest, batch slowest) of the 8 x 8 x 30 grid.
 __device__ __forceinline__ TileOrigin ws_origin(const TileGrid& t, int T) {
     const unsigned u = (unsigned)T;
     const unsigned q1 = (unsigned)(((unsigned long long)u * t.mx) >> t.sx);
@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_pull_ws(const __grid_constant
     }
 }
 
-// Tile grid of 8 x 8 x 15 tiles over the sample grid (all batches), with the
+// Tile grid of 8 x 8 x 30 tiles over the sample grid (all batches), with the
 // multiply-shift constants of ws_origin.
 TileGrid ws_make_grid(const LaunchArgs& a) {
     TileGrid t;

@@ -35,7 +35,7 @@ def tiles(pkg):
             assert lib.pp_get_tile(op, d, *[C.byref(x) for x in v]) == 0
             saved[(op, d)] = [x.value for x in v]
     # degree 1 onto the tiled kernels as well (pull: the warp-specialised code)
-    assert lib.pp_set_tile(0, 1, 3, 3, 4, 9216) == 0, lib.pp_last_error()
+    assert lib.pp_set_tile(0, 1, 3, 3, 4, 15360) == 0, lib.pp_last_error()
     assert lib.pp_set_tile(3, 1, 3, 3, 3, 16384) == 0, lib.pp_last_error()
     yield lib
     for (op, d), v in saved.items():
@@ -95,7 +95,7 @@ def test_affine_tiled_vs_oracle(pkg, O, tiles, deg, bnd, ext, zoom):
 def test_affine_tiled_degree0_bit_exact(pkg, O, tiles):
     """Nearest neighbour through the tiled paths is bit-exact against the reference rounding."""
     lib = tiles
-    assert lib.pp_set_tile(0, 0, 3, 3, 4, 9216) == 0 and lib.pp_set_tile(3, 0, 3, 3, 3, 16384) == 0
+    assert lib.pp_set_tile(0, 0, 3, 3, 4, 15360) == 0 and lib.pp_set_tile(3, 0, 3, 3, 3, 16384) == 0
     rng = np.random.default_rng(7)
     d0, d1 = (40, 36, 32), (40, 36, 32)
     A = _map(rng, d0, d1, zoom=1.1)

@@ -1,4 +1,4 @@
-"""The warp-specialised pull kernels (8 x 8 x 15 tiles; fifteen consumer warps
+"""The warp-specialised pull kernels (8 x 8 x 30 tiles; fifteen consumer warps
 evaluate while one producer warp streams the deformation and stages interior
 boxes) against the FP64 oracle, on every path they take:
 
@@ -35,7 +35,7 @@ def ws(pkg):
             assert lib.pp_get_tile(op, d, *[C.byref(x) for x in v]) == 0
             saved[(op, d)] = [x.value for x in v]
     for op in (0, 1):
-        assert lib.pp_set_tile(op, -1, 3, 3, 4, 9216) == 0, lib.pp_last_error()
+        assert lib.pp_set_tile(op, -1, 3, 3, 4, 15360) == 0, lib.pp_last_error()
     yield lib
     for (op, d), v in saved.items():
         lib.pp_set_tile(op, d, *v)
