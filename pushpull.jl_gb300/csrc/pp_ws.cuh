@@ -337,6 +337,9 @@ __device__ __forceinline__ void ws_pull_unit(const LaunchArgs& a, const TileOrig
     const Geometry& g = a.g;
     const long long n1 = g.n1;
     const bool last = c == g.nc - 1;
+    // the box record in registers: the output stores would otherwise make the
+    // compiler reload it from shared memory for every voxel
+    const int bmode = box.mode, bxo = box.xo, by0 = box.lo[1], bz0 = box.lo[2], bP = box.P, bQ = box.Q;
     auto voxel = [&](int q) {
         const int lin = ctid + q * kWsCons;
         const IT v = ws_index<IT>(o, lin, D0, D1, D2);
@@ -350,17 +353,17 @@ __device__ __forceinline__ void ws_pull_unit(const LaunchArgs& a, const TileOrig
             }
             return;
         }
-        if (box.mode == 2) {   // box larger than a buffer: every channel from global memory, once
+        if (bmode == 2) {   // box larger than a buffer: every channel from global memory, once
             if (c == 0) pull_voxel_lean<DP, OP_, IT>(a, o.b, (long long)v, x0, x1, x2);
             return;
         }
-        if (box.mode != 1) return;
+        if (bmode != 1) return;
         W3<DP, ORD> wx, wy, wz;
-        const int ox = spline_taps32<DP, ORD>(x0, wx.w, wx.dw, wx.hw) - box.xo;
-        const int oy = spline_taps32<DP, ORD>(x1, wy.w, wy.dw, wy.hw) - box.lo[1];
-        const int oz = spline_taps32<DP, ORD>(x2, wz.w, wz.dw, wz.hw) - box.lo[2];
-        const unsigned P4 = 4u * box.P, Q4 = 4u * box.Q;
-        const unsigned p = smem_addr(sm) + 4u * (unsigned)(oz * box.Q + oy * box.P + ox);
+        const int ox = spline_taps32<DP, ORD>(x0, wx.w, wx.dw, wx.hw) - bxo;
+        const int oy = spline_taps32<DP, ORD>(x1, wy.w, wy.dw, wy.hw) - by0;
+        const int oz = spline_taps32<DP, ORD>(x2, wz.w, wz.dw, wz.hw) - bz0;
+        const unsigned P4 = 4u * bP, Q4 = 4u * bQ;
+        const unsigned p = smem_addr(sm) + 4u * (unsigned)(oz * bQ + oy * bP + ox);
         float r[6];
         contract_smem<OP, DP>(wx, wy, wz, p, P4, Q4, r);
         if constexpr (pull_is_dot<OP_>()) {
