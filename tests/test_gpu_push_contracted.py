@@ -68,3 +68,36 @@ def test_contracted_push_vs_oracle(pkg, O, deg, ext):
         lib.pp_set_path(0)
     for c in (0, 2, 3, 4, 5):
         assert rel_err(got[..., c, :], direct[..., c, :]) <= 1e-4, c
+
+
+@pytest.mark.parametrize("deg", [3, 2])
+def test_contracted_push_grad_vs_oracle(pkg, O, deg):
+    """push_grad on contracted tiles (records of v0 dw_x, v1 w_x, v2 w_x and the
+    y and z weights and derivatives), per-channel bounds, a channel of zeros and
+    one beyond the fixed-point range, against FP64 and the per-voxel kernels."""
+    L = pkg.layout
+    rng = np.random.default_rng(700 + deg)
+    d, nb, nc = (44, 40, 36), 2, 3
+    phi = _phi(O, rng, d, 0.2, 0.4, nb)
+    g = rng.standard_normal(d + (3, nc, nb))
+    g[..., 1, :] = 0.0
+    g[..., 2, :] *= 1e30
+    g = np.asfortranarray(g.astype(np.float32))
+    bnd = [(1, 1, 1), (0, 1, 2), (2, 0, 1)]
+    s, so = pkg.Settings(deg, bnd, 1), O.Sett.make(deg, bnd, 1)
+    got = L.to_numpy(pkg.push_grad(L.from_numpy(g), L.from_numpy(phi), d, s))
+    lib = pkg.native_library()
+    assert lib.pp_device_status(1) == 0
+    ref = O.push_grad(g, phi, d, so)
+    for b in range(nb):
+        assert not np.any(got[..., 1, b])
+        for c in (0, 2):
+            assert np.isfinite(got[..., c, b]).all()
+            assert rel_err(got[..., c, b], ref[..., c, b]) <= 1e-4, (c, b)
+    assert lib.pp_set_path(1) == 0
+    try:
+        direct = L.to_numpy(pkg.push_grad(L.from_numpy(g), L.from_numpy(phi), d, s))
+    finally:
+        lib.pp_set_path(0)
+    for c in (0, 2):
+        assert rel_err(got[..., c, :], direct[..., c, :]) <= 1e-4, c

@@ -118,3 +118,16 @@ def test_ws_falls_back_when_tma_cannot_stream_phi(pkg, O, ws):
     f0 = np.asfortranarray(rng.standard_normal(d0).astype(np.float32))
     phi = _phi(O, rng, d1, d0, 1.0)
     _check(pkg, O, f0, phi, 3, 1, 1)
+
+
+@pytest.mark.parametrize("z", [14, 15, 16, 31, 61])
+def test_ws_sample_depths_around_the_tile(pkg, O, ws, z):
+    """Sample grids 14..61 deep against 30-deep tiles: 15 or more take the
+    warp-specialised kernels (partial last tiles), 14 the block-synchronous ones;
+    pull and pull_grad agree with FP64 either way."""
+    rng = np.random.default_rng(600 + z)
+    d0, d1 = (40, 32, z + 4), (40, 32, z)
+    f0 = np.asfortranarray(rng.standard_normal(d0 + (2, 2)).astype(np.float32))
+    phi = _phi(O, rng, d1, d0, 1.2, nb=2)
+    _check(pkg, O, f0, phi, 3, [(1, 1, 1), (2, 0, 1)], 1)
+    _check(pkg, O, f0, phi, 2, 0, 0)
