@@ -231,11 +231,12 @@ enum pp_path { PP_PATH_AUTO = 0, PP_PATH_DIRECT = 1 };
  * shared-memory budget of its image footprint box in floats, for one op
  * (-1: all ops) and one isotropic degree (-1: all degrees).  cap_floats == 0
  * selects the per-voxel kernels for that (op, degree); this is the default for
- * degrees 0 and 1, where gathering straight from L2 beats staging a box.  The
+ * degree 0 and for the push family, pull_hess and the fused step at degree 1,
+ * where gathering straight from L2 beats staging a box.  The
  * code (lx, ly, lz) = (3, 3, 4) selects, for pull and pull_grad, the
  * warp-specialised kernels (one producer warp streams the deformation and
  * stages footprint boxes by TMA while fifteen consumer warps evaluate 8x8x30
- * tiles; their box budget is fixed); it is the default at degrees 2..4.  No
+ * tiles; their box budget is fixed); it is the default at degrees 1..4.  No
  * reference counterpart (the reference launches one thread per voxel with no
  * tiling, ext/pushpull_gpu.jl:386-391); used by the autotuner. */
 int pp_set_tile(int op, int deg, int lx, int ly, int lz, int cap_floats);
