@@ -231,9 +231,10 @@ enum pp_path { PP_PATH_AUTO = 0, PP_PATH_DIRECT = 1 };
  * shared-memory budget of its image footprint box in floats, for one op
  * (-1: all ops) and one isotropic degree (-1: all degrees).  cap_floats == 0
  * selects the per-voxel kernels for that (op, degree); this is the default for
- * degree 0 and for the push family, pull_hess and the fused step at degree 1,
- * where gathering straight from L2 beats staging a box.  The
- * code (lx, ly, lz) = (3, 3, 4) selects, for pull and pull_grad, the
+ * degree 0 and for the push family and the fused step at degree 1, where
+ * gathering straight from L2 beats staging a box.  The code (lx, ly, lz) =
+ * (3, 3, 4) selects, for pull, pull_grad and pull_hess (and through their
+ * entries pull_grad_dot and pull_hess_dot), the
  * warp-specialised kernels (one producer warp streams the deformation and
  * stages footprint boxes by TMA while fifteen consumer warps evaluate 8x8x30
  * tiles; their box budget is fixed); it is the default at degrees 1..4.  No

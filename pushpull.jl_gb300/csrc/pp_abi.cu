@@ -104,18 +104,20 @@ void init_tiles_locked() {
     // 8x8x8 tiles; the push family keeps two words per accumulator element; the
     // fused step's 2560-float budget at degree 2 leaves room for three CTAs per SM.
     // Degrees 0 and 1 (one or two taps per axis) default to the per-voxel
-    // kernels (cap 0; pull and pull_grad at degree 1 are set below): with so few
+    // kernels (cap 0; the pull family at degree 1 is set below): with so few
     // taps, gathering through L2 is faster than a block-synchronous staging of
     // a footprint box (192^3, GB300: pull 0.10 vs 0.16 ms, push 0.13 vs
     // 0.24 ms, fused step 0.29 vs 0.40 ms at degree 1).
     for (int op = 0; op < 6; ++op)
         for (int d = 0; d < 5; ++d)
             g_tiles[op][d] = TileCfg{3, 3, 3, d <= 1 ? 0 : (op < 3 ? 8192 : (op < 5 ? 16384 : (d == 2 ? 2560 : 4096)))};
-    // pull and pull_grad at degrees 1..4: the warp-specialised kernels
-    // (192^3, GB300, against the next best family: cubic pull 0.179 vs 0.254 ms,
-    // pull_grad 0.198 vs 0.262 ms; linear pull 0.084 vs 0.095 ms and pull_grad
-    // 0.095 vs 0.144 ms against the per-voxel kernels)
-    for (int op = 0; op < 2; ++op)
+    // pull, pull_grad and pull_hess (with the dot ops, which share their
+    // entries) at degrees 1..4: the warp-specialised kernels (192^3, GB300,
+    // against the next best family: cubic pull 0.179 vs 0.254 ms, pull_grad
+    // 0.198 vs 0.262 ms, pull_hess 0.222 vs 0.285 ms, pull_grad_dot 0.201 vs
+    // 0.271 ms, pull_hess_dot 0.236 vs 0.298 ms; linear pull 0.084 vs 0.095 ms,
+    // pull_grad 0.095 vs 0.144 ms, pull_hess 0.117 vs 0.177 ms)
+    for (int op = 0; op < 3; ++op)
         for (int d = 1; d < 5; ++d) g_tiles[op][d] = TileCfg{3, 3, 4, 15360};
     g_tiles_init = true;
 }

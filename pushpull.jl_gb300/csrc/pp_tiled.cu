@@ -18,6 +18,9 @@ unsigned status_push_grad(bool reset);
 unsigned status_fused(bool reset);
 unsigned status_batch(bool reset);
 unsigned status_ws_pull(bool reset);
+unsigned status_ws_hess(bool reset);
+unsigned status_ws_grad_dot(bool reset);
+unsigned status_ws_hess_dot(bool reset);
 unsigned status_push_affine(bool reset);
 
 bool tiled_supported(const LaunchArgs& a, const TileCfg& t) {
@@ -99,6 +102,9 @@ unsigned read_device_status(bool reset) {
     v |= status_fused(reset);
     v |= status_batch(reset);
     v |= status_ws_pull(reset);
+    v |= status_ws_hess(reset);
+    v |= status_ws_grad_dot(reset);
+    v |= status_ws_hess_dot(reset);
     v |= status_push_affine(reset);
     v |= unit_status(reset);   // the bounded-wait probe of this unit
     return v;

@@ -324,13 +324,14 @@ __device__ __forceinline__ void ws_mirror_fixup(const Box& box, const Geometry& 
     }
 }
 
-// One consumer thread, one (tile, channel) unit of the pull family: its two
-// voxels against the staged box (dot ops accumulate into acc and store after
-// the last channel).
+// One consumer thread, one (tile, channel) unit of the pull family: its four
+// voxels against the staged box.  The dot ops accumulate over channels in the
+// output itself: channel 0 writes its term, later channels (same thread, same
+// voxels) read it back and add theirs, in the order the per-voxel kernels
+// accumulate in registers.
 template <int DP, int OP_, typename IT, class POS>
 __device__ __forceinline__ void ws_pull_unit(const LaunchArgs& a, const TileOrigin& o, int ctid, const POS& pos,
-                                             int c, const Box& box, const float* sm, float (&acc)[kWsV][3], int D0,
-                                             int D1, int D2) {
+                                             int c, const Box& box, const float* sm, int D0, int D1, int D2) {
     constexpr int OP = pull_base_op<OP_>();
     constexpr int NCOMP = pull_ncomp<OP_>();
     constexpr int ORD = op_order(OP);
@@ -367,24 +368,23 @@ __device__ __forceinline__ void ws_pull_unit(const LaunchArgs& a, const TileOrig
         float r[6];
         contract_smem<OP, DP>(wx, wy, wz, p, P4, Q4, r);
         if constexpr (pull_is_dot<OP_>()) {
-            dot_accumulate<OP_>(a, o.b, c, (long long)v, r, acc[q]);
-            if (last) {
-                float* out = pull_out<OP_>(a, o.b, 0, (long long)v);
-                out[0] = acc[q][0];
-                out[n1] = acc[q][1];
-                out[2 * n1] = acc[q][2];
+            float* out = pull_out<OP_>(a, o.b, 0, (long long)v);
+            float acc[3] = {0.f, 0.f, 0.f};
+            if (c > 0) {
+                acc[0] = out[0];
+                acc[1] = out[n1];
+                acc[2] = out[2 * n1];
             }
+            dot_accumulate<OP_>(a, o.b, c, (long long)v, r, acc);
+            out[0] = acc[0];
+            out[n1] = acc[1];
+            out[2 * n1] = acc[2];
         } else {
             pull_store<OP>(pull_out<OP_>(a, o.b, c, (long long)v), n1, r);
         }
     };
-    if constexpr (pull_is_dot<OP_>()) {
-#pragma unroll
-        for (int q = 0; q < kWsV; ++q) voxel(q);
-    } else {
 #pragma unroll 1
-        for (int q = 0; q < kWsV; ++q) voxel(q);
-    }
+    for (int q = 0; q < kWsV; ++q) voxel(q);
 }
 
 // AFF: the affine pull -- no deformation ring; positions from `aff`.
@@ -513,9 +513,6 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_pull_ws(const __grid_constant
         const WsPos<AFF> pos{ring + (j % kWsStages) * 3 * kWsNV, &aff};
         if (j + 1 < ntl && !publish_bounds(j + 1)) s_abort = 1;
         if (s_abort) break;
-        float acc[kWsV][3];
-#pragma unroll
-        for (int q = 0; q < kWsV; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.f;
         for (int c = 0; c < nc; ++c) {
             const int q = j * nc + c, b = q % kWsBufs, k = q / kWsBufs;
             if (!mbar_wait(box_full + 8u * b, (unsigned)(k & 1))) s_abort = 1;
@@ -533,7 +530,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_pull_ws(const __grid_constant
                     asm volatile("bar.sync 1, %0;" ::"n"(kWsCons) : "memory");
                 }
             }
-            ws_pull_unit<DP, OP, IT>(a, o, ctid, pos, c, box, buf, acc, D0, D1, D2);
+            ws_pull_unit<DP, OP, IT>(a, o, ctid, pos, c, box, buf, D0, D1, D2);
             __syncwarp();
             if (lane == 0) mbar_arrive(box_empty + 8u * b);
         }
@@ -622,6 +619,25 @@ cudaError_t launch_ws_one(const LaunchArgs& a, const TileGrid& t, const CUtensor
     const int grid = tt.ntiles < sm_count() ? tt.ntiles : sm_count();
     kern<<<grid, kWsThreads, kWsSmem, s>>>(a, tt, phimap, imgmap, aff);
     return cudaGetLastError();
+}
+
+template <int OP, typename IT, bool AFF = false>
+cudaError_t ws_dispatch(const LaunchArgs& a, const TileGrid& t, const CUtensorMap& phimap, cudaStream_t s,
+                        const AffineMap& aff = AffineMap{}) {
+    switch (a.g.dp[0]) {
+        case 1: return launch_ws_one<1, OP, IT, AFF>(a, t, phimap, aff, s);
+        case 2: return launch_ws_one<2, OP, IT, AFF>(a, t, phimap, aff, s);
+        case 3: return launch_ws_one<3, OP, IT, AFF>(a, t, phimap, aff, s);
+        case 4: return launch_ws_one<4, OP, IT, AFF>(a, t, phimap, aff, s);
+        default: return launch_ws_one<5, OP, IT, AFF>(a, t, phimap, aff, s);
+    }
+}
+
+// One op of the warp-specialised family on 32-bit or 64-bit voxel indices.
+template <int OP>
+cudaError_t ws_dispatch_op(const LaunchArgs& a, const TileGrid& t, const CUtensorMap& phimap, cudaStream_t s) {
+    const bool small = a.g.n0 < (1LL << 31) - 1 && a.g.n1 < (1LL << 31) - 1;
+    return small ? ws_dispatch<OP, int>(a, t, phimap, s) : ws_dispatch<OP, long long>(a, t, phimap, s);
 }
 
 }  // namespace

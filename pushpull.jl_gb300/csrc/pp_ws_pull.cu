@@ -1,21 +1,14 @@
-// pp_ws_pull.cu -- warp-specialised pull and pull_grad kernels (pp_ws.cuh).
+// pp_ws_pull.cu -- warp-specialised pull family (pp_ws.cuh): pull, pull_grad and
+// the affine pull here; pull_hess and the dot ops in their own translation units
+// (pp_ws_hess.cu, pp_ws_grad_dot.cu, pp_ws_hess_dot.cu) so that they compile in
+// parallel.
 #include "pp_ws.cuh"
 
 namespace pp {
 
-namespace {
-template <int OP, typename IT, bool AFF = false>
-cudaError_t ws_dispatch(const LaunchArgs& a, const TileGrid& t, const CUtensorMap& phimap, cudaStream_t s,
-                        const AffineMap& aff = AffineMap{}) {
-    switch (a.g.dp[0]) {
-        case 1: return launch_ws_one<1, OP, IT, AFF>(a, t, phimap, aff, s);
-        case 2: return launch_ws_one<2, OP, IT, AFF>(a, t, phimap, aff, s);
-        case 3: return launch_ws_one<3, OP, IT, AFF>(a, t, phimap, aff, s);
-        case 4: return launch_ws_one<4, OP, IT, AFF>(a, t, phimap, aff, s);
-        default: return launch_ws_one<5, OP, IT, AFF>(a, t, phimap, aff, s);
-    }
-}
-}  // namespace
+cudaError_t launch_ws_hess(const LaunchArgs& a, const TileGrid& t, const CUtensorMap& phimap, cudaStream_t s);
+cudaError_t launch_ws_grad_dot(const LaunchArgs& a, const TileGrid& t, const CUtensorMap& phimap, cudaStream_t s);
+cudaError_t launch_ws_hess_dot(const LaunchArgs& a, const TileGrid& t, const CUtensorMap& phimap, cudaStream_t s);
 
 bool ws_supported(const LaunchArgs& a) {
     const Geometry& g = a.g;
@@ -35,11 +28,14 @@ cudaError_t launch_ws_pull(int op, const LaunchArgs& a, cudaStream_t s) {
     CUtensorMap phimap;
     std::memset(&phimap, 0, sizeof phimap);
     if (!encode_ws_phi_map(&phimap, a.phi, a.g.d1, 3LL * a.g.nb)) return cudaErrorNotSupported;
-    const bool small = a.g.n0 < (1LL << 31) - 1 && a.g.n1 < (1LL << 31) - 1;
-    if (op == kPull) return small ? ws_dispatch<kPull, int>(a, t, phimap, s) : ws_dispatch<kPull, long long>(a, t, phimap, s);
-    if (op == kPullGrad)
-        return small ? ws_dispatch<kPullGrad, int>(a, t, phimap, s) : ws_dispatch<kPullGrad, long long>(a, t, phimap, s);
-    return cudaErrorNotSupported;
+    switch (op) {
+        case kPull: return ws_dispatch_op<kPull>(a, t, phimap, s);
+        case kPullGrad: return ws_dispatch_op<kPullGrad>(a, t, phimap, s);
+        case kPullHess: return launch_ws_hess(a, t, phimap, s);
+        case kPullGradDot: return launch_ws_grad_dot(a, t, phimap, s);
+        case kPullHessDot: return launch_ws_hess_dot(a, t, phimap, s);
+        default: return cudaErrorNotSupported;
+    }
 }
 
 // Affine pull (pp_pull_affine) on the same kernels, positions computed in place.

@@ -1,6 +1,7 @@
 """The warp-specialised pull kernels (8 x 8 x 30 tiles; fifteen consumer warps
 evaluate while one producer warp streams the deformation and stages interior
-boxes) against the FP64 oracle, on every path they take:
+boxes) against the FP64 oracle, on every path they take, for pull, pull_grad,
+pull_hess and the two cotangent contractions (pull_grad_dot, pull_hess_dot):
 
 * interior boxes staged by one TMA copy of the fixed window;
 * boundary boxes gathered by the consumers with folding and DST-II signs, with
@@ -34,7 +35,7 @@ def ws(pkg):
             v = [C.c_int() for _ in range(4)]
             assert lib.pp_get_tile(op, d, *[C.byref(x) for x in v]) == 0
             saved[(op, d)] = [x.value for x in v]
-    for op in (0, 1):
+    for op in (0, 1, 2):
         assert lib.pp_set_tile(op, -1, 3, 3, 4, 15360) == 0, lib.pp_last_error()
     yield lib
     for (op, d), v in saved.items():
@@ -131,3 +132,48 @@ def test_ws_sample_depths_around_the_tile(pkg, O, ws, z):
     phi = _phi(O, rng, d1, d0, 1.2, nb=2)
     _check(pkg, O, f0, phi, 3, [(1, 1, 1), (2, 0, 1)], 1)
     _check(pkg, O, f0, phi, 2, 0, 0)
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3, 4])
+def test_ws_hessian_and_dot_ops(pkg, O, ws, deg):
+    """pull_hess, pull_grad_dot and pull_hess_dot on the warp-specialised kernels
+    (the dot ops sum their channels in the output array): two channels with
+    per-channel bounds, a batch of two, interior and boundary boxes, against FP64
+    and against the per-voxel kernels on the same inputs."""
+    L = pkg.layout
+    lib = pkg.native_library()
+    rng = np.random.default_rng(800 + deg)
+    d0 = d1 = (40, 36, 44)
+    nb = 2
+    f0 = np.asfortranarray(rng.standard_normal(d0 + (2, nb)).astype(np.float32))
+    phi = _phi(O, rng, d1, d0, 1.5, nb=nb)
+    ug = np.asfortranarray(rng.standard_normal(d1 + (2, nb)).astype(np.float32))
+    uh = np.asfortranarray(rng.standard_normal(d1 + (3, 2, nb)).astype(np.float32))
+    bnd = [(0, 1, 2), (2, 2, 1)]
+    s, so = pkg.Settings(deg, bnd, 1), O.Sett.make(deg, bnd, 1)
+    tf0, tphi, tug, tuh = (L.from_numpy(x) for x in (f0, phi, ug, uh))
+
+    def run():
+        out = (pkg.pull_hess(tf0, tphi, s), pkg.pull_grad_dot(tf0, tphi, tug, s), pkg.pull_hess_dot(tf0, tphi, tuh, s))
+        torch.cuda.synchronize()
+        return [L.to_numpy(x) for x in out]
+
+    got_h, got_gd, got_hd = run()
+    assert lib.pp_device_status(1) == 0
+    assert got_h.shape == d1 + (3, 3, 2, nb) and got_gd.shape == phi.shape and got_hd.shape == phi.shape
+    for b in range(nb):
+        fb, pb = np.asfortranarray(f0[..., b]), np.asfortranarray(phi[..., b])
+        h = O.pull_hess(fb, pb, so, threads=8)                    # (d1, 3, 3, C)
+        g = O.pull_grad(fb, pb, so, threads=8)                    # (d1, 3, C)
+        assert rel_err(got_h[..., b], h) <= 1e-4, (deg, b)
+        ref_gd = np.einsum("xyzkc,xyzc->xyzk", g, ug[..., b].astype(np.float64))
+        assert rel_err(got_gd[..., b], ref_gd) <= 1e-4, (deg, b)
+        ref_hd = np.einsum("xyzpqc,xyzqc->xyzp", h, uh[..., b].astype(np.float64))
+        assert rel_err(got_hd[..., b], ref_hd) <= 1e-4, (deg, b)
+    assert lib.pp_set_path(1) == 0
+    try:
+        direct = run()
+    finally:
+        lib.pp_set_path(0)
+    for got, ref in zip((got_h, got_gd, got_hd), direct):
+        assert rel_err(got, ref) <= 1e-5
