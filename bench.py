@@ -594,13 +594,14 @@ def contention_leg(pkg, dev, args):
 
 
 PROFILE_CASES = ("pull", "pull_grad", "push", "affine_pull", "affine_push", "contention_push",
-                 "contention_push_grad", "fused")
+                 "contention_push_grad", "fused", "nearest_pull", "pull_hess_dot")
 
 
 def run_profile(args):
     """Launch one op on its benchmark workload --warmup + --steps times, untimed:
-    the program the ncu captures run (192^3 cubic for pull, pull_grad, push and the
-    affine ops; the 256^3 x 3 contraction for contention_*; the 160x192x160
+    the program the ncu captures run (192^3 cubic for pull, pull_grad, push,
+    pull_hess_dot and the affine ops; the same deformation at degree 0 for
+    nearest_pull; the 256^3 x 3 contraction for contention_*; the 160x192x160
     quadratic step for fused)."""
     import torch
     import __graft_entry__ as entry
@@ -635,7 +636,12 @@ def run_profile(args):
         f1 = pkg.pull(f0, phi, s)
         Aff = W.affine_map(d0, seed=args.seed + 4)
         out0, out1, outg = L.empty(d0, device=dev), L.empty(d1, device=dev), L.empty(d1 + (3,), device=dev)
+        s0 = pkg.Settings(0, w.bnd, w.ext)
+        up = L.empty(d1 + (3,), device=dev)
+        up.copy_(torch.randn(up.shape, generator=torch.Generator(device=dev).manual_seed(54), device=dev))
         fn = {"pull": lambda: pkg.pull(f0, phi, s, out=out1),
+              "nearest_pull": lambda: pkg.pull(f0, phi, s0, out=out1),
+              "pull_hess_dot": lambda: pkg.pull_hess_dot(f0, phi, up, s),
               "pull_grad": lambda: pkg.pull_grad(f0, phi, s, out=outg),
               "push": lambda: pkg.push(f1, phi, d0, s, out=out0, accumulate=False),
               "affine_pull": lambda: pkg.affine_pull(f0, Aff, d1, s, out=out1),
