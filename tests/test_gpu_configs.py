@@ -71,13 +71,18 @@ def tiles(pkg):
     lib.pp_set_path(0)
 
 
-@pytest.mark.parametrize("family", ["default", "tiled"])
+@pytest.mark.parametrize("family", ["default", "tiled", "direct"])
 def test_c1_all_ops_vs_oracle(pkg, O, W, tiles, family):
+    """The 64^3 trilinear workload on each kernel family: the defaults
+    (warp-specialised pull and pull_grad, per-voxel push), the block-synchronous
+    tiled kernels, and the per-voxel kernels for every op."""
     L = pkg.layout
     w = W.config1()
     if family == "tiled":
         for op, cap in ((0, 8192), (1, 8192), (3, 16384), (4, 16384)):
             assert tiles.pp_set_tile(op, 1, 3, 3, 3, cap) == 0
+    elif family == "direct":
+        assert tiles.pp_set_path(1) == 0
     s, so = pkg.Settings(w.deg, w.bnd, w.ext), O.Sett.make(w.deg, w.bnd, w.ext)
     d = w.f0.shape[:3]
     f1 = np.asfortranarray(W.image(d, 11))
