@@ -83,3 +83,30 @@ def test_native_errors_raise(pkg):
     with pytest.raises(TypeError, match="CUDA"):
         pkg.pull(L.zeros((4, 4, 4), device="cpu"), L.zeros((4, 4, 4, 3), device="cpu"), s)
     assert torch.float32 == L.zeros((2, 2, 2), device="cpu").dtype
+
+
+def test_default_kernel_routing(pkg):
+    """The tile registry's defaults, per (op, degree): op 0 pull, 1 pull_grad (and
+    pull_grad_dot), 2 pull_hess (and pull_hess_dot), 3 push, 4 push_grad, 5 the
+    fused step.  (3, 3, 4) selects the warp-specialised pull family, cap 0 the
+    per-voxel kernels (the nearest-neighbour kernel for pull at degree 0), other
+    shapes the block-synchronous tiled kernels with that box budget."""
+    lib = pkg.native_library()
+
+    def tile(op, deg):
+        v = [C.c_int() for _ in range(4)]
+        assert lib.pp_get_tile(op, deg, *[C.byref(x) for x in v]) == 0
+        return tuple(x.value for x in v)
+
+    ws = (3, 3, 4, 15360)
+    for op in (0, 1, 2):
+        assert tile(op, 0)[3] == 0
+        for deg in (1, 2, 3, 4):
+            assert tile(op, deg) == ws, (op, deg)
+    for op in (3, 4, 5):
+        assert tile(op, 0)[3] == 0 and tile(op, 1)[3] == 0, op
+    for op in (3, 4):
+        for deg in (2, 3, 4):
+            assert tile(op, deg) == (3, 3, 3, 16384), (op, deg)
+    assert tile(5, 2) == (3, 3, 3, 2560)
+    assert tile(5, 3) == (3, 3, 3, 4096) and tile(5, 4) == (3, 3, 3, 4096)
