@@ -1,10 +1,13 @@
-// pp_ws.cuh -- warp-specialised persistent pull family.
+// pp_ws.cuh -- warp-specialised persistent pull family: pull, pull_grad,
+// pull_hess, the rrule contractions pull_grad_dot / pull_hess_dot, and the
+// affine pull.
 //
-// Included after pp_tiled_impl.cuh (whose helpers it uses) by pp_ws_pull.cu.
+// Included after pp_tiled_impl.cuh (whose helpers it uses) by pp_ws_pull.cu,
+// pp_ws_hess.cu, pp_ws_grad_dot.cu and pp_ws_hess_dot.cu.
 //
 // One CTA per SM: 15 consumer warps and one producer warp (512 threads, so
 // every thread keeps 128 registers).  The CTA walks tiles of 8 x 8 x 30 sample
-// voxels, two per consumer thread, in (tile, channel) units:
+// voxels, four per consumer thread, in (tile, channel) units:
 //   * the producer warp streams each tile's deformation into a ring of
 //     shared-memory slots with one TMA copy per tile (mbarrier complete_tx);
 //   * every consumer warp reduces the first taps of its own voxels of tile
@@ -22,8 +25,10 @@
 // Interior units therefore pass no CTA-wide barrier at all.  Boxes larger than
 // a buffer take the per-voxel global path for that tile.
 //
-// Reference kernels replaced: pull_element / pullg_element (artifacts/C/pushpull.cu:33-79);
-// per-voxel math pull1 / pullg1 (artifacts/C/pushpull_dev.cu:61-88).
+// Reference kernels replaced: pull_element / pullg_element / pullh_element
+// (artifacts/C/pushpull.cu:33-109); per-voxel math pull1 / pullg1 / pullh1
+// (artifacts/C/pushpull_dev.cu:61-117); the rrule contractions replace the
+// pull_grad and pull_hess temporaries of the rrules (src/pushpull_pb.jl:11-35).
 #pragma once
 
 #include "pp_tiled_impl.cuh"
