@@ -625,6 +625,35 @@ void infer_sample_grid(const pp_usize* d0, pp_usize n1, pp_usize d1[3]) {
     }
 }
 
+// z-slab boundaries zb[0..n] of a sample grid of `planes` z-planes of `plane`
+// voxels; returns n <= kSlabs.  Large slabs hold at least 1 Mi voxels; the last
+// ones halve down to about an eighth of a large slab, because computing a plane
+// takes less time than copying its inputs in, so only the last (small) slab's
+// kernels, and for the pull family its copy back, remain after the last input
+// has arrived.  Grids under 2 Mi voxels are one slab.
+int slab_bounds(pp_usize planes, pp_usize plane, pp_usize* zb) {
+    zb[0] = 0;
+    const pp_usize min_planes = plane ? ((1u << 20) + plane - 1) / plane : planes;
+    if (planes < 2 || planes * plane < (2u << 20)) {
+        zb[1] = planes;
+        return 1;
+    }
+    pp_usize big = (planes + kSlabs - 4) / (kSlabs - 3);
+    if (big < min_planes) big = min_planes;
+    pp_usize size[kSlabs];
+    int n = 0;
+    pp_usize sum = 0, t = big / 8 ? big / 8 : 1;
+    while (sum < planes && n < kSlabs) {   // from the back: t, 2t, 4t, ... up to big
+        pp_usize sz = t < big ? t : big;
+        if (n == kSlabs - 1 || sz > planes - sum) sz = planes - sum;
+        size[n++] = sz;
+        sum += sz;
+        t *= 2;
+    }
+    for (int k = 0; k < n; ++k) zb[k + 1] = zb[k] + size[n - 1 - k];
+    return n;
+}
+
 // kind: 0 pull, 1 pullg, 2 pullh, 3 push, 4 pushg.  The sample grid is cut into
 // up to kSlabs z-slabs: slab k's inputs are copied (h2d stream) while slab k-1
 // is computed (kernel stream) and slab k-2's results are copied back (d2h
@@ -663,13 +692,12 @@ int compat_call(int kind, float* out, const float* phi, const float* in, const p
     if (e != cudaSuccess) return pp::cuda_fail(e, "copy shared input");
     if ((e = cudaEventRecord(w.in_ready, w.h2d)) != cudaSuccess) return pp::cuda_fail(e, "event");
     if ((e = cudaStreamWaitEvent(w.stream, w.in_ready, 0)) != cudaSuccess) return pp::cuda_fail(e, "wait");
-    // slabs of whole z-planes, at least 1 Mi voxels each
+    // slabs of whole z-planes
     const pp_usize plane = d1[0] * d1[1];
-    pp_usize nslab = d1[2] < (pp_usize)kSlabs ? d1[2] : (pp_usize)kSlabs;
-    while (nslab > 1 && (d1[2] / nslab) * plane < (1u << 20)) --nslab;
-    if (nslab < 1) nslab = 1;
-    for (pp_usize k = 0; k < nslab; ++k) {
-        const pp_usize z0 = d1[2] * k / nslab, z1 = d1[2] * (k + 1) / nslab;
+    pp_usize zb[kSlabs + 1];
+    const int nslab = slab_bounds(d1[2], plane, zb);
+    for (int k = 0; k < nslab; ++k) {
+        const pp_usize z0 = zb[k], z1 = zb[k + 1];
         const pp_usize off = z0 * plane, ns = (z1 - z0) * plane;
         if (ns == 0) continue;
         // slab inputs, compact: phi (ns, 3) at dphi + 3 off; push values (ns, comps) at din + comps off
