@@ -65,3 +65,28 @@ def test_fd_gradient_wrt_phi(O, deg):
     ana = np.einsum("xyzc,xyzkc->xyzk", 2 * r, gr)
     fd = _fd_phi_pull(O, f1, f2, phi, s)
     assert np.sum((ana - fd) ** 2) / np.sum(ana ** 2) < 1e-3
+
+
+@pytest.mark.parametrize("deg", [3, 4])
+def test_hessian_is_jacobian_of_gradient(O, deg):
+    """pull_hess against central differences of pull_grad in the sample position
+    (the pair the pull_grad rrule chains, src/pushpull_pb.jl:26-35): splines of
+    degree 3 and 4 are C^2, positions inside the image, two channels with
+    different bounds; relative error below 1e-3."""
+    rng = np.random.default_rng(40 + deg)
+    d = (11, 10, 9)
+    f = np.asfortranarray(rng.standard_normal(d + (2,)).astype(np.float32))
+    phi = np.empty(d + (3,), dtype=np.float32, order="F")
+    for k in range(3):
+        phi[..., k] = rng.uniform(3.0, d[k] - 2.0, d).astype(np.float32)
+    s = O.Sett.make(deg, [(1, 1, 1), (2, 0, 1)], 1)
+    H = O.pull_hess(f, phi, s)                                # (d, 3, 3, C)
+    assert np.allclose(H, np.swapaxes(H, 3, 4), rtol=0, atol=1e-10 * np.abs(H).max())
+    fd = np.zeros_like(H)
+    for q in range(3):
+        pp, pm = phi.copy(order="F"), phi.copy(order="F")
+        pp[..., q] = (phi[..., q] + np.float32(0.002)).astype(np.float32)
+        pm[..., q] = (phi[..., q] - np.float32(0.002)).astype(np.float32)
+        step = (pp[..., q].astype(np.float64) - pm[..., q].astype(np.float64))[..., None, None]
+        fd[..., :, q, :] = ((O.pull_grad(f, pp, s) - O.pull_grad(f, pm, s)) / step)
+    assert np.sqrt(np.sum((H - fd) ** 2) / np.sum(H ** 2)) < 1e-3
